@@ -1,0 +1,405 @@
+#!/usr/bin/env python
+"""FlOF on GB300: 4D flow solves/s at 64^4 to a fixed CG residual.
+
+One step is the whole two-way workload at one resolution:
+  * both deformations (data 0 -> 1 and 1 -> 0) with opticalFlowMultiscale4d
+    at 64^4 float32, flof.py's parameters with cgAccuracy 1e-4;
+  * the mode-2 two-way apply (deform4d) at alpha 0.25 / 0.5 / 0.75 on the
+    64^4 grid;
+  * the mode-3 two-way apply (loadAdvectTimeSlice_OptRun for both
+    directions plus the blend) of every frame of a 128^3 x 64 hi-res SDF
+    series at the same three alphas.
+Inputs are the seeded synthetic drop/pool SDFs of ofblend_gb300.synth.
+
+value: solves/s with inputs resident in HBM (2 solves per step, summed over
+ranks); e2e: the same through the C ABI with host buffers, copies included.
+`--impl reference` times the CPU oracle (a restatement of the reference's
+CPU path) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "4D flow solves/s at 64^4 to fixed residual: learned warm-start vs plain CG"
+UNIT = "solves/s"
+ALPHAS = (0.25, 0.5, 0.75)
+
+
+def args_():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--res", type=int, default=64)
+    ap.add_argument("--hires", type=int, default=128)
+    ap.add_argument("--cg-accuracy", type=float, default=1e-4)
+    ap.add_argument("--blur-type", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def flof_params(acc, blur_type):
+    # scenes/flof.py:913-915 with ofsd defaults, except the CG accuracy
+    return dict(wSmooth=0.001, wEnergy=0.0001, cgAccuracy=acc, postVelBlur=4, cfl=999, multiStep=3,
+                minGridSize=20, doFinalProject=True, resetBndWidth=0.1, blurType=blur_type)
+
+
+def dist():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid: str | None):
+        self.uuid = uuid
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=5)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            if self.uuid and self.uuid not in f[1]:
+                continue
+            try:
+                sm.append(float(f[2]))
+                mx.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class Workload:
+    def __init__(self, F, synth, R, H, acc, blur_type, ctx):
+        self.F = F
+        self.R, self.H = R, H
+        self.Tf = R  # hi-res frames = t extent of the deformation
+        dims = (R, R, R, R)
+        self.dims = dims
+        s0, s1 = synth.scene_for(0), synth.scene_for(1)
+        self.h_i0 = synth.flow_input(s0, dims)
+        self.h_i1 = synth.flow_input(s1, dims)
+        self.h_s0 = synth.sdf4d(s0, dims)
+        self.h_s1 = synth.sdf4d(s1, dims)
+        hd = (H, H, H, self.Tf)
+        self.h_hi0 = synth.sdf4d(s0, hd)
+        self.h_hi1 = synth.sdf4d(s1, hd)
+        self.params = flof_params(acc, blur_type)
+        mk = lambda cls, d: cls(dims=d, ctx=ctx)  # noqa: E731
+        self.g_i0, self.g_i1 = mk(F.Grid4Real, dims), mk(F.Grid4Real, dims)
+        self.g_s0, self.g_s1 = mk(F.Grid4Real, dims), mk(F.Grid4Real, dims)
+        self.g_hi0, self.g_hi1 = mk(F.Grid4Real, hd), mk(F.Grid4Real, hd)
+        self.v01, self.v10 = mk(F.Grid4Vec4, dims), mk(F.Grid4Vec4, dims)
+        self.out4 = mk(F.Grid4Real, dims)
+        self.dst = mk(F.RealGrid, (H, H, H, 1))
+        self.factor = (H / R, H / R, H / R, self.Tf / R)
+        self.bord = int(H * 0.1)
+        self.stats = []
+
+    def upload(self, pinned=None):
+        src = pinned or {}
+        for name in ("i0", "i1", "s0", "s1", "hi0", "hi1"):
+            getattr(self, "g_" + name).from_numpy(src.get(name, getattr(self, "h_" + name)))
+
+    def h2d_bytes(self):
+        return sum(getattr(self, "h_" + n).nbytes for n in ("i0", "i1", "s0", "s1", "hi0", "hi1"))
+
+    def step(self, sink=None):
+        F = self.F
+        self.v01.clear()
+        self.v10.clear()
+        F.opticalFlowMultiscale4d(self.v01, self.g_i0, self.g_i1, **self.params)
+        self.stats.append(F.last_solve_stats())
+        F.opticalFlowMultiscale4d(self.v10, self.g_i1, self.g_i0, **self.params)
+        self.stats.append(F.last_solve_stats())
+        if sink is not None:
+            self.v01.to_numpy(sink["v01"])
+            self.v10.to_numpy(sink["v10"])
+        for a in ALPHAS:
+            F.deform4d(self.out4, self.g_s0, self.g_s1, self.v01, self.v10, alpha=a, twoway=1)
+            if sink is not None:
+                self.out4.to_numpy(sink["out4"])
+        F.loadAdvectTimeSlice_OptInit(1, self.v01)
+        F.loadAdvectTimeSlice_OptInit(2, self.v10)
+        H, Tf = self.H, self.Tf
+        for a in ALPHAS:
+            for t in range(Tf):
+                F.loadAdvectTimeSlice_OptRunTwoway(1, 2, self.dst, self.g_hi0, self.g_hi1, t + 0.5, a, 1.0,
+                                                   (0, 0, 0, 0), (1, 1, 1, Tf / Tf), self.factor,
+                                                   overrideSize=(H, H, H, Tf), overrideTimeOff=0.0,
+                                                   bordSkip=self.bord)
+                if sink is not None:
+                    self.dst.to_numpy(sink["frame"])
+        F.loadAdvectTimeSlice_Finish(1)
+        F.loadAdvectTimeSlice_Finish(2)
+
+    def d2h_bytes(self):
+        return (2 * self.v01.dims[0] ** 4 * 16 + len(ALPHAS) * self.h_s0.nbytes
+                + len(ALPHAS) * self.Tf * self.H ** 3 * 4)
+
+
+def roofline(records, R, peak, peak_kind, traffic):
+    per = {}
+    for name, sx, nb, ms in records:
+        if sx != R:
+            continue
+        e = per.setdefault(name, [0, 0.0, 0.0])
+        e[0] += 1
+        e[1] += nb
+        e[2] += ms
+    if not per:
+        return None, {}
+    dom = max(per, key=lambda k: per[k][2])
+    n, nb, ms = per[dom]
+    achieved = (nb / n) / ((ms / n) * 1e-3) / 1e9
+    tr = traffic.get(dom)
+    rl = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+          "frac": round(achieved / peak, 4), "traffic": tr, "kernel": dom,
+          "launches": n, "bytes_per_launch": nb / n, "ms_per_launch": ms / n,
+          "peak_source": f"hbm_gbs of {peak_kind}"}
+    share = {k: {"launches": v[0], "ms": round(v[2], 3),
+                 "GBps": round(v[1] / (v[2] * 1e-3) / 1e9, 1) if v[2] > 0 else None} for k, v in per.items()}
+    return rl, share
+
+
+def cpu_sample_seconds(acc, threads_note=True):
+    """One full flof solve 0 -> 1 at 32^4 on the host with the oracle."""
+    import oracle
+    from ofblend_gb300 import synth
+    o = oracle.get(False)
+    dims = (32, 32, 32, 32)
+    i0 = synth.flow_input(synth.scene_for(0), dims)
+    i1 = synth.flow_input(synth.scene_for(1), dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    p = flof_params(acc, 1)
+    p.pop("blurType")
+    t = time.perf_counter()
+    o.opticalFlowMultiscale4d(zv, i0, i1, **p)
+    return time.perf_counter() - t
+
+
+CPU_SAMPLE = ("one full opticalFlowMultiscale4d 0->1 at 32^4 (flof parameters, same cgAccuracy) per step; "
+              "64^4 solves/s = 1/(16 * t_32): the cell ratio, which matches the reference's own 64^4/32^4 "
+              "time ratio of 15.9 measured at cgAccuracy 0.01")
+
+
+def run_gpu(a):
+    import torch
+    rank, world, local = dist()
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    import ofblend_gb300 as F
+    from ofblend_gb300 import synth
+    ctx = F.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    W = Workload(F, synth, a.res, a.hires, a.cg_accuracy, a.blur_type, ctx)
+    W.upload()
+    for _ in range(max(a.warmup, 0)):
+        W.step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    uuid = None
+    try:
+        uuid = str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    clocks = ClockSampler(uuid)
+    clocks.start()
+    W.stats.clear()
+    ctx.profile(True)
+    l0 = ctx.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(a.steps):
+        W.step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.kernel_launches() - l0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    recs = ctx.profile_records()
+    ctx.profile(False)
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    solves = 2 * a.steps * world
+    value = solves / (ms_max * 1e-3)
+    peak, peak_kind = measured_peaks()
+    rl, share = roofline(recs, a.res, peak, peak_kind, ncu_traffic())
+
+    # e2e: through the C ABI with pinned host buffers, copies inside
+    pinned = {}
+    for n in ("i0", "i1", "s0", "s1", "hi0", "hi1"):
+        h = getattr(W, "h_" + n)
+        tt = torch.empty(h.shape, dtype=torch.float32, pin_memory=True)
+        tt.numpy()[...] = h
+        pinned[n] = tt.numpy()
+    sink = {"v01": torch.empty(W.v01.shape, dtype=torch.float32, pin_memory=True).numpy(),
+            "v10": torch.empty(W.v10.shape, dtype=torch.float32, pin_memory=True).numpy(),
+            "out4": torch.empty(W.out4.shape, dtype=torch.float32, pin_memory=True).numpy(),
+            "frame": torch.empty(W.dst.shape, dtype=torch.float32, pin_memory=True).numpy()}
+    W.upload(pinned)
+    W.step(sink)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        W.upload(pinned)
+        W.step(sink)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_val = 2 * a.e2e_steps * world / float(te.item())
+
+    st = W.stats
+    iters = [s["solves"] for s in st]
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(ms_max / a.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded drop/pool SDFs)",
+        "config": {"workload": f"two-way FlOF at {a.res}^4: both deformations (flof parameters, "
+                               f"cgAccuracy {a.cg_accuracy}, blurType {a.blur_type}) + deform4d and "
+                               f"{a.hires}^3x{a.res} hi-res frames at alpha 0.25/0.5/0.75",
+                   "grid": [a.res] * 4, "hires": [a.hires] * 3 + [a.res], "frames_per_step": 3 * a.res,
+                   "solver": "plain multiscale Jacobi-PCG", "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": rl,
+        "e2e": {"value": round(e2e_val, 4), "unit": UNIT, "h2d_bytes_per_step": W.h2d_bytes(),
+                "d2h_bytes_per_step": W.d2h_bytes(), "steps": a.e2e_steps},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "kernel_share": share,
+        "cg_iterations_level0": [[x[1] for x in s if x[0] == a.res] for s in iters[:2]],
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        t32 = cpu_sample_seconds(a.cg_accuracy)
+        line["cpu_baseline"] = {"value": round(1.0 / (16.0 * t32), 6), "unit": UNIT,
+                                "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                                "sample": CPU_SAMPLE, "seconds": round(t32, 3)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(a):
+    rank, world, _ = dist()
+    if rank != 0:
+        return
+    times = []
+    for _ in range(max(a.warmup, 0)):
+        cpu_sample_seconds(a.cg_accuracy)
+    for _ in range(a.steps):
+        times.append(cpu_sample_seconds(a.cg_accuracy))
+    t32 = sum(times) / len(times)
+    v = 1.0 / (16.0 * t32)
+    cores = int(os.environ["OMP_NUM_THREADS"])
+    line = {
+        "metric": METRIC, "value": round(v, 6), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(t32 * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded drop/pool SDFs)",
+        "impl": "reference",
+        "config": {"workload": f"two-way FlOF at {a.res}^4 (CPU oracle, bounded sample)",
+                   "grid": [a.res] * 4, "parallelism": f"{cores} host threads"},
+        "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": CPU_SAMPLE},
+        "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = args_()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gpu(a)

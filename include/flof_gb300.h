@@ -1,0 +1,274 @@
+/*
+ * flof_gb300.h -- C ABI of the GB300 implementation of the FlOF hot path
+ * (thunil/ofblend, source/plugin/optflow4d.cpp and the Grid4d type of
+ * source/grid4d.{h,cpp}).
+ *
+ * Every entry point is a plain C function over opaque handles, plain
+ * pointers and sizes; none throws.  Each returns an flof_status and, on
+ * failure, leaves a message retrievable with flof_last_error() (thread
+ * local).  The reference raises a C++ exception through errMsg()
+ * (source/general.h:96-99) which its Python wrapper turns into a Python
+ * error; a binding maps a non-zero status to its own error type.
+ *
+ * Data layout is the reference's (source/grid4d.h:92-97): a 4D grid of size
+ * (X,Y,Z,T) is stored x-fastest, idx = i + X*j + X*Y*k + X*Y*Z*t.  Real
+ * grids hold one float per cell, Vec4 grids four (x,y,z,t interleaved).  A
+ * 3D Grid<Real> (the mode-3 output slice) is a grid with T == 1.
+ *
+ * Grids live in device memory (HBM) and are owned by a context, as the
+ * reference's grids are owned by a FluidSolver pool
+ * (source/fluidsolver.cpp:87-124).  Host buffers enter and leave through
+ * flof_grid_upload / flof_grid_download.  All work of one context runs in
+ * order on the context's CUDA stream; calls that return scalars (errors,
+ * maxima) synchronise on that stream.  A context is used by one thread at a
+ * time, like the reference's plugins, which run with the Python GIL held.
+ */
+#ifndef FLOF_GB300_H
+#define FLOF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLOF_API __attribute__((visibility("default")))
+
+typedef enum {
+  FLOF_OK = 0,
+  FLOF_E_ARG = 1,      /* invalid argument, size or type mismatch         */
+  FLOF_E_CUDA = 2,     /* CUDA runtime error                               */
+  FLOF_E_OOM = 3,      /* device allocation failed                         */
+  FLOF_E_NAN = 4,      /* non-finite values where finite ones are required */
+  FLOF_E_STALL = 5,    /* iterative solve stopped without converging       */
+  FLOF_E_TIMEOUT = 6,  /* a bounded device wait gave up                    */
+  FLOF_E_STATE = 7,    /* call out of order (e.g. OptRun before OptInit)   */
+  FLOF_E_NOTFOUND = 8  /* unknown handle or id                             */
+} flof_status;
+
+/* Element types, numbered as Grid4dBase::Grid4dType (source/grid4d.h:29-35). */
+typedef enum { FLOF_REAL = 1, FLOF_VEC4 = 8 } flof_elem;
+
+/* Gaussian blur variants for postVelBlur (optflow4d.cpp:531-541).
+ * 1 = the reference's direct 4D stencil (knGaussianBlur, :132-158), bitwise
+ *     equal to the reference;
+ * 2 = separable 4x1D stencil with the same in-bounds normalisation, equal
+ *     to 1 up to float rounding and several times cheaper. */
+enum { FLOF_BLUR_GAUSS = 1, FLOF_BLUR_GAUSS_SEPARABLE = 2 };
+
+typedef struct flof_ctx flof_ctx;
+typedef struct flof_grid flof_grid;
+
+/* Keyword arguments of opticalFlowMultiscale4d
+ * (optflow4d.cpp:2182-2189), same names and meaning, plus cgMaxIter, which
+ * the reference hard-codes to 1000 (:502). */
+typedef struct flof_of_params {
+  float wSmooth;
+  float wEnergy;
+  int level;
+  float postVelBlur;
+  float cgAccuracy;
+  int blurType;
+  float cfl;
+  int orderTime;
+  int orderSpace;
+  float resetBndWidth;
+  int multiStep;
+  int projSizeThresh;
+  int minGridSize;
+  int doFinalProject;
+  int cgMaxIter;
+  int reserved[7];
+} flof_of_params;
+
+#define FLOF_MAX_SOLVE_STATS 64
+/* Per-call record of the linear solves (the reference logs the same facts
+ * with debMsg, optflow4d.cpp:496-517). */
+typedef struct flof_solve_stats {
+  int nsolves;
+  int size_x[FLOF_MAX_SOLVE_STATS];     /* X extent of the level            */
+  int iterations[FLOF_MAX_SOLVE_STATS]; /* PCG iterations                   */
+  float residual[FLOF_MAX_SOLVE_STATS]; /* max(r)/max(r0) at exit           */
+  int status[FLOF_MAX_SOLVE_STATS];     /* 1 converged, 2 sigma==0/NaN,
+                                           3 tiny initial residual,
+                                           4 iteration limit                */
+  int cg_total_iterations;
+  int syncs;                            /* host synchronisations            */
+  float err_final;                      /* returned error metric            */
+  double seconds;                       /* wall time of the call            */
+} flof_solve_stats;
+
+/* ---- library / context -------------------------------------------------- */
+FLOF_API const char *flof_version(void);
+FLOF_API const char *flof_last_error(void);
+FLOF_API const char *flof_status_string(int status);
+/* Fills the reference's defaults of opticalFlowMultiscale4d
+ * (optflow4d.cpp:2182-2189), cgMaxIter = 1000, blurType = 1. */
+FLOF_API void flof_of_params_default(flof_of_params *p);
+/* Fills the parameters scenes/flof.py:913-915 passes in mode 1. */
+FLOF_API void flof_of_params_flof(flof_of_params *p);
+
+FLOF_API int flof_ctx_create(int device, flof_ctx **out);
+FLOF_API int flof_ctx_destroy(flof_ctx *ctx);
+FLOF_API int flof_ctx_synchronize(flof_ctx *ctx);
+/* Use an external CUDA stream (cudaStream_t passed as void*); NULL restores
+ * the context's own stream. */
+FLOF_API int flof_ctx_set_stream(flof_ctx *ctx, void *stream);
+FLOF_API void *flof_ctx_stream(flof_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+FLOF_API long long flof_ctx_kernel_launches(flof_ctx *ctx);
+/* Kernel tracing.  flof_ctx_profile(ctx, 1) clears the record list and
+ * brackets every later kernel launch with CUDA events on the context stream;
+ * each record holds the kernel class, the X extent of the launch's grid, its
+ * algorithmic bytes (compulsory reads + writes) and its device time.  The
+ * reference times whole plugin calls instead (pbPreparePlugin /
+ * pbFinalizePlugin, source/pwrapper/pclass.cpp:27-45). */
+FLOF_API int flof_ctx_profile(flof_ctx *ctx, int enable);
+FLOF_API int flof_ctx_profile_count(flof_ctx *ctx, int *n);
+FLOF_API int flof_ctx_profile_record(flof_ctx *ctx, int i, int *cls,
+                                     int *size_x, double *bytes, float *ms);
+FLOF_API const char *flof_kernel_class_name(int cls);
+/* Release cached device buffers of the context's pool. */
+FLOF_API int flof_ctx_trim(flof_ctx *ctx);
+
+/* ---- grids: Grid4d<Real>, Grid4d<Vec4> (source/grid4d.h:117-265) -------- */
+/* New zero-filled device grid (the Grid4d constructor clears, grid4d.cpp:82). */
+FLOF_API int flof_grid_create(flof_ctx *ctx, const int dims[4], int elem,
+                              flof_grid **out);
+/* Non-owning view of caller device memory (x-fastest, 16-byte aligned). */
+FLOF_API int flof_grid_wrap(flof_ctx *ctx, const int dims[4], int elem,
+                            void *device_ptr, flof_grid **out);
+FLOF_API int flof_grid_destroy(flof_grid *g);
+FLOF_API int flof_grid_dims(const flof_grid *g, int dims[4], int *elem);
+FLOF_API void *flof_grid_data(flof_grid *g);
+/* Host <-> device copies of the whole grid (bytes = cells * 4 * ncomp). */
+FLOF_API int flof_grid_upload(flof_grid *g, const void *host);
+FLOF_API int flof_grid_download(const flof_grid *g, void *host);
+
+/* Grid4d methods (grid4d.cpp:198-412).  Constants are float[4]; Real grids
+ * use element 0. */
+FLOF_API int flof_grid_copyFrom(flof_grid *dst, const flof_grid *src);
+FLOF_API int flof_grid_add(flof_grid *a, const flof_grid *b);
+FLOF_API int flof_grid_sub(flof_grid *a, const flof_grid *b);
+FLOF_API int flof_grid_setConst(flof_grid *a, const float v[4]);
+FLOF_API int flof_grid_addConst(flof_grid *a, const float v[4]);
+FLOF_API int flof_grid_multConst(flof_grid *a, const float v[4]);
+FLOF_API int flof_grid_addScaled(flof_grid *a, const flof_grid *b,
+                                 const float factor[4]);
+FLOF_API int flof_grid_clear(flof_grid *a);
+/* getMax / getMin / getMaxAbs (grid4d.cpp:263-285); Vec4 grids reduce the
+ * vector norm. */
+FLOF_API int flof_grid_getMax(flof_grid *a, float *out);
+FLOF_API int flof_grid_getMin(flof_grid *a, float *out);
+FLOF_API int flof_grid_getMaxAbs(flof_grid *a, float *out);
+/* setBound: cells with c <= w or c >= size-1-w (knSetBnd4d, :355-368). */
+FLOF_API int flof_grid_setBound(flof_grid *a, const float v[4], int w);
+/* setBoundNeumann (knSetBnd4dNeumann, :370-407). */
+FLOF_API int flof_grid_setBoundNeumann(flof_grid *a, int w);
+
+/* ---- plugins --------------------------------------------------------------- */
+
+/* opticalFlowMultiscale4d (optflow4d.cpp:2182-2195 ->
+ * opticalFlowMultiscaleTemplate :936-1173).  vel is in/out (flof passes a
+ * zero grid); i0, i1 are Real grids of the same size.  err (nullable)
+ * receives the returned error metric; stats (nullable) the solve record.
+ * rhsT of the reference is a debug output and is not offered. */
+FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *ctx, flof_grid *vel,
+                                          const flof_grid *i0,
+                                          const flof_grid *i1,
+                                          const flof_of_params *params,
+                                          float *err, flof_solve_stats *stats);
+
+/* opticalFlow4d (optflow4d.cpp:2110-2119 -> opticalFlowDim :361-553): one
+ * level, one solve.  iterations / residual (nullable) report the PCG. */
+FLOF_API int flof_opticalFlow4d(flof_ctx *ctx, flof_grid *vel,
+                                const flof_grid *i0, const flof_grid *i1,
+                                float wSmooth, float wEnergy, float postVelBlur,
+                                float cgAccuracy, int blurType,
+                                float resetBndWidth, int cgMaxIter,
+                                int *iterations, float *residual);
+
+/* corrVelsOf4d (optflow4d.cpp:2121-2130 -> corrVelsOfTempl :737-802).
+ * phiCurr is unused by the reference and may be NULL. */
+FLOF_API int flof_corrVelsOf4d(flof_ctx *ctx, flof_grid *dst, flof_grid *vel,
+                               const flof_grid *phiOrg,
+                               const flof_grid *phiCurr,
+                               const flof_grid *phiTarget, float threshPhi,
+                               float threshNorm, float postVelBlur,
+                               float resetBndWidth, int maxIter);
+
+/* gaussianBlurGeneric(a, sigma, iter=1) (optflow4d.cpp:160-174), the
+ * reference's internal velocity blur, exposed for stage-wise checks.
+ * blurType as in flof_of_params (1 direct stencil, 2 separable). */
+FLOF_API int flof_gaussianBlur4d(flof_ctx *ctx, flof_grid *a, float sigma,
+                                 int blurType);
+
+/* advect4d (optflow4d.cpp:1292-1306): semi-Lagrangian advection of a Real
+ * or Vec4 grid by vel with dt = solver dt (1) * dtFac. */
+FLOF_API int flof_advect4d(flof_ctx *ctx, const flof_grid *vel,
+                           flof_grid *grid, float dtFac);
+
+/* calcLsDiff4d (optflow4d.cpp:2132-2137 -> calcLsDiffTempl :895-927). */
+FLOF_API int flof_calcLsDiff4d(flof_ctx *ctx, const flof_grid *i0,
+                               const flof_grid *i1, flof_grid *out,
+                               float correction, int bnd, float *result);
+
+/* interpolateGrid4d / interpolateGrid4dVec (grid4d.cpp:540-557).  offset,
+ * scale and size are float[4] (defaults 0, 1, -1). */
+FLOF_API int flof_interpolateGrid4d(flof_ctx *ctx, flof_grid *target,
+                                    const flof_grid *source,
+                                    const float offset[4], const float scale[4],
+                                    const float size[4]);
+FLOF_API int flof_interpolateGrid4dVec(flof_ctx *ctx, flof_grid *target,
+                                       const flof_grid *source,
+                                       const float offset[4],
+                                       const float scale[4],
+                                       const float size[4]);
+
+/* Mode-2 apply of scenes/flof.py deform4d (:591-615) into `out`:
+ * twoway 0: out = advect4d(vel, i0, alpha)
+ * twoway 1: out = advect(vel,i0,alpha)*(1-alpha) + alpha*advect(velInv,i1,1-alpha)
+ * twoway 2: out = advect(vel,i0,alpha)*(1-alpha) + alpha*i1  (naive blend)
+ * alphaInv is the float (1 - alpha) the scene computes in double. */
+FLOF_API int flof_deform4d(flof_ctx *ctx, flof_grid *out, const flof_grid *i0,
+                           const flof_grid *i1, const flof_grid *vel,
+                           const flof_grid *velInv, float alpha,
+                           float alphaInv, int twoway);
+
+/* loadAdvectTimeSlice_OptInit (optflow4d.cpp:1871-1913).  The reference
+ * names a .uni file that OptRun streams t-slices from; here the whole
+ * deformation `defo` (Vec4 grid) is already resident in device memory and
+ * the context keeps a reference to it until Finish.  Defo volumes
+ * (useDefoVols, the three-data-set mode) are not supported: FLOF_E_ARG. */
+FLOF_API int flof_loadAdvectTimeSlice_OptInit(flof_ctx *ctx, int id,
+                                              const flof_grid *defo,
+                                              int useDefoVols, int doAligned,
+                                              float partialLoadFac);
+/* loadAdvectTimeSlice_OptRun (optflow4d.cpp:1951-2105) for one output frame:
+ * blends defo t-slices t and t+1, then knSemiLagrangeLookupSlice4d_WithVel
+ * (:1648-1665) writes dst (a T == 1 grid) inside the bnd=10 / bordSkip box.
+ * Vector arguments are float[4]. */
+FLOF_API int flof_loadAdvectTimeSlice_OptRun(
+    flof_ctx *ctx, int id, flof_grid *dst, const flof_grid *phi, float time,
+    float blendAlpha, float loadTimeScale, const float defoOffset[4],
+    const float defoScale[4], const float defoFactor[4],
+    const float overrideSize[4], float overrideTimeOff, int zeroVel,
+    float thirdAlpha, int bordSkip, float fourthAlpha, float defoAniFac);
+/* Two-way frame in one pass: dst = OptRun(id0, phi0, alpha) * (1-alpha) +
+ * alpha * OptRun(id1, phi1, 1-alpha), the blend of scenes/flof.py:750-755.
+ * Cells outside the lookup box keep their previous contents (the scene
+ * overwrites that ring with setBound afterwards, flof.py:830-832). */
+FLOF_API int flof_loadAdvectTimeSlice_OptRunTwoway(
+    flof_ctx *ctx, int id0, int id1, flof_grid *dst, const flof_grid *phi0,
+    const flof_grid *phi1, float time, float blendAlpha, float alphaInv,
+    float loadTimeScale, const float defoOffset[4], const float defoScale[4],
+    const float defoFactor[4], const float overrideSize[4],
+    float overrideTimeOff, int bordSkip, float defoAniFac);
+/* loadAdvectTimeSlice_Finish (optflow4d.cpp:1930-1950). */
+FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *ctx, int id);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLOF_GB300_H */

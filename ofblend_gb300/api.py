@@ -1,0 +1,474 @@
+"""The reference's Python call surface for the FlOF path, backed by the CUDA
+library.
+
+scenes/flof.py drives the reference through mantaflow's Python bindings:
+``Solver(...)`` with ``solv.create(Grid4Real / Grid4Vec4 / RealGrid)``, the
+Grid4d methods (source/grid4d.h:205-236) and the plugins
+``opticalFlowMultiscale4d``, ``advect4d``, ``calcLsDiff4d``,
+``interpolateGrid4d(Vec)``, ``loadAdvectTimeSlice_Opt*`` and helpers from
+source/plugin/optflow4d.cpp and source/grid4d.cpp.  This module offers the
+same names, keyword arguments and defaults, so a flof.py-shaped driver runs
+with a changed import.  Grids live in GPU memory; ``to_numpy`` /
+``from_numpy`` move their contents (layout x fastest, arrays shaped
+(T, Z, Y, X) or (T, Z, Y, X, 4)).
+
+Errors surface as FlofError (a RuntimeError), as the reference's errMsg
+exceptions surface as Python errors.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import FLOF_REAL, FLOF_VEC4, FlofError, OFParams, SolveStats, check, f4
+
+__all__ = [
+    "FlofError", "Context", "context", "Solver", "Grid4Real", "Grid4Vec4", "RealGrid",
+    "vec3", "vec4", "Vec3", "Vec4",
+    "opticalFlowMultiscale4d", "opticalFlow4d", "corrVelsOf4d", "advect4d", "calcLsDiff4d",
+    "gaussianBlur4d",
+    "interpolateGrid4d", "interpolateGrid4dVec", "deform4d",
+    "loadAdvectTimeSlice_OptInit", "loadAdvectTimeSlice_OptRun",
+    "loadAdvectTimeSlice_OptRunTwoway", "loadAdvectTimeSlice_Finish", "last_solve_stats",
+]
+
+
+# ---------------------------------------------------------------------------
+# small vector types (the scenes use vec3 / vec4 / Vec3 / Vec4)
+# ---------------------------------------------------------------------------
+class vec4:
+    def __init__(self, x=0.0, y=None, z=None, t=None):
+        if y is None:
+            y = z = t = x
+        self.x, self.y, self.z, self.t = float(x), float(y), float(z if z is not None else 0.0), \
+            float(t if t is not None else 0.0)
+
+    def __iter__(self):
+        return iter((self.x, self.y, self.z, self.t))
+
+    def __repr__(self):
+        return f"vec4({self.x}, {self.y}, {self.z}, {self.t})"
+
+
+class vec3(vec4):
+    def __init__(self, x=0.0, y=None, z=None):
+        if y is None:
+            y = z = x
+        super().__init__(x, y, z if z is not None else 0.0, 0.0)
+
+    def __iter__(self):
+        return iter((self.x, self.y, self.z))
+
+    def __repr__(self):
+        return f"vec3({self.x}, {self.y}, {self.z})"
+
+
+Vec3 = vec3
+Vec4 = vec4
+
+
+# ---------------------------------------------------------------------------
+# context
+# ---------------------------------------------------------------------------
+class Context:
+    """One flof_ctx: a CUDA stream plus a device buffer pool on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.lib()
+        h = ctypes.c_void_p()
+        check(self.lib.flof_ctx_create(int(device), ctypes.byref(h)))
+        self.h = h
+        self.device = device
+
+    def synchronize(self):
+        check(self.lib.flof_ctx_synchronize(self.h))
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.flof_ctx_kernel_launches(self.h))
+
+    def set_stream(self, stream_handle: int | None):
+        check(self.lib.flof_ctx_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    def trim(self):
+        check(self.lib.flof_ctx_trim(self.h))
+
+    def profile(self, enable: bool = True):
+        """Start (clearing old records) or stop per-launch event tracing."""
+        check(self.lib.flof_ctx_profile(self.h, int(bool(enable))))
+
+    def profile_records(self):
+        """[(kernel class, grid X extent, algorithmic bytes, device ms)]."""
+        n = ctypes.c_int()
+        check(self.lib.flof_ctx_profile_count(self.h, ctypes.byref(n)))
+        out = []
+        cls, sx, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        nb = ctypes.c_double()
+        names = {}
+        for i in range(n.value):
+            check(self.lib.flof_ctx_profile_record(self.h, i, ctypes.byref(cls), ctypes.byref(sx),
+                                                   ctypes.byref(nb), ctypes.byref(ms)))
+            if cls.value not in names:
+                names[cls.value] = self.lib.flof_kernel_class_name(cls.value).decode()
+            out.append((names[cls.value], sx.value, nb.value, ms.value))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.flof_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def context() -> Context:
+    """The process-wide default context on cuda:0 (created on first use)."""
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+# ---------------------------------------------------------------------------
+# grids
+# ---------------------------------------------------------------------------
+class _Grid:
+    ELEM = FLOF_REAL
+    NC = 1
+
+    def __init__(self, parent: "Solver" | None = None, dims=None, ctx: Context | None = None,
+                 data_ptr: int | None = None, name: str = ""):
+        self.ctx = ctx or (parent.ctx if parent is not None else context())
+        if dims is None:
+            if parent is None:
+                raise FlofError(1, "a grid needs a parent solver or explicit dims")
+            dims = parent.grid_dims(self._is3d())
+        self.dims = tuple(int(a) for a in dims)
+        self.name = name
+        h = ctypes.c_void_p()
+        cd = (ctypes.c_int * 4)(*self.dims)
+        L = self.ctx.lib
+        if data_ptr is None:
+            check(L.flof_grid_create(self.ctx.h, cd, self.ELEM, ctypes.byref(h)))
+        else:
+            check(L.flof_grid_wrap(self.ctx.h, cd, self.ELEM, ctypes.c_void_p(data_ptr), ctypes.byref(h)))
+        self.h = h
+
+    @staticmethod
+    def _is3d():
+        return False
+
+    # -- sizes ------------------------------------------------------------------
+    def getSizeX(self): return self.dims[0]
+    def getSizeY(self): return self.dims[1]
+    def getSizeZ(self): return self.dims[2]
+    def getSizeT(self): return self.dims[3]
+
+    def getSize(self):
+        return vec4(*self.dims)
+
+    @property
+    def shape(self):
+        X, Y, Z, T = self.dims
+        return (T, Z, Y, X, 4) if self.NC == 4 else (T, Z, Y, X)
+
+    def data_ptr(self) -> int:
+        return int(self.ctx.lib.flof_grid_data(self.h) or 0)
+
+    # -- host transfer ----------------------------------------------------------
+    def from_numpy(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if a.size != int(np.prod(self.shape)):
+            raise FlofError(1, f"array of {a.size} floats does not fit grid {self.dims} x {self.NC}")
+        check(self.ctx.lib.flof_grid_upload(self.h, a.ctypes.data_as(ctypes.c_void_p)))
+        return self
+
+    def to_numpy(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.shape, dtype=np.float32)
+        check(self.ctx.lib.flof_grid_download(self.h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    # -- Grid4d methods (grid4d.h:205-236) --------------------------------------
+    def copyFrom(self, a, copyType=True):
+        check(self.ctx.lib.flof_grid_copyFrom(self.h, a.h))
+        return self
+
+    def add(self, a):
+        check(self.ctx.lib.flof_grid_add(self.h, a.h))
+
+    def sub(self, a):
+        check(self.ctx.lib.flof_grid_sub(self.h, a.h))
+
+    def setConst(self, s):
+        check(self.ctx.lib.flof_grid_setConst(self.h, f4(s)))
+
+    def addConst(self, s):
+        check(self.ctx.lib.flof_grid_addConst(self.h, f4(s)))
+
+    def multConst(self, s):
+        check(self.ctx.lib.flof_grid_multConst(self.h, f4(s)))
+
+    def addScaled(self, a, factor):
+        check(self.ctx.lib.flof_grid_addScaled(self.h, a.h, f4(factor)))
+
+    def clear(self):
+        check(self.ctx.lib.flof_grid_clear(self.h))
+
+    def _reduce(self, fn):
+        out = ctypes.c_float()
+        check(fn(self.h, ctypes.byref(out)))
+        return float(out.value)
+
+    def getMax(self):
+        return self._reduce(self.ctx.lib.flof_grid_getMax)
+
+    def getMin(self):
+        return self._reduce(self.ctx.lib.flof_grid_getMin)
+
+    def getMaxAbs(self):
+        return self._reduce(self.ctx.lib.flof_grid_getMaxAbs)
+
+    getMaxValue = getMax
+    getMinValue = getMin
+    getMaxAbsValue = getMaxAbs
+
+    def setBound(self, value, boundaryWidth=1):
+        check(self.ctx.lib.flof_grid_setBound(self.h, f4(value), int(boundaryWidth)))
+
+    def setBoundNeumann(self, boundaryWidth=1):
+        check(self.ctx.lib.flof_grid_setBoundNeumann(self.h, int(boundaryWidth)))
+
+    def free(self):
+        if getattr(self, "h", None) is not None:
+            self.ctx.lib.flof_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Grid4Real(_Grid):
+    """Grid4d<Real>."""
+    ELEM = FLOF_REAL
+    NC = 1
+
+
+class Grid4Vec4(_Grid):
+    """Grid4d<Vec4>."""
+    ELEM = FLOF_VEC4
+    NC = 4
+
+
+class RealGrid(_Grid):
+    """A 3D Grid<Real> (t extent 1), the output of the mode-3 slice lookup."""
+    ELEM = FLOF_REAL
+    NC = 1
+
+    @staticmethod
+    def _is3d():
+        return True
+
+    @property
+    def shape(self):
+        X, Y, Z, _ = self.dims
+        return (Z, Y, X)
+
+
+class Solver:
+    """FluidSolver stand-in: holds the grid size, the 4th dimension and dt
+    (source/fluidsolver.h), and creates grids on the GPU."""
+
+    def __init__(self, name="main", gridSize=None, dim=3, fourthDim=-1, ctx: Context | None = None):
+        if gridSize is None:
+            raise FlofError(1, "Solver needs gridSize")
+        self.name = name
+        gs = list(gridSize)
+        self.gridSize = (int(gs[0]), int(gs[1]), int(gs[2]))
+        self.dim = dim
+        self.fourthDim = int(fourthDim)
+        self.timestep = 1.0
+        self.ctx = ctx or context()
+
+    def grid_dims(self, is3d=False):
+        X, Y, Z = self.gridSize
+        T = 1 if is3d else max(self.fourthDim, 1)
+        return (X, Y, Z, T)
+
+    def create(self, cls, name=""):
+        return cls(self, name=name)
+
+    def getDt(self):
+        return self.timestep
+
+    def step(self):
+        pass
+
+
+# ---------------------------------------------------------------------------
+# plugins
+# ---------------------------------------------------------------------------
+_last_stats: dict | None = None
+
+
+def last_solve_stats() -> dict | None:
+    """The solve record of the last opticalFlowMultiscale4d call."""
+    return _last_stats
+
+
+def _ctx_of(g) -> Context:
+    return g.ctx
+
+
+def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
+                            cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
+                            resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
+                            doFinalProject=False, cgMaxIter=1000):
+    """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
+    error metric (the reference's template returns it to C++ callers)."""
+    global _last_stats
+    p = OFParams()
+    _lib.lib().flof_of_params_default(ctypes.byref(p))
+    p.wSmooth, p.wEnergy, p.level = wSmooth, wEnergy, int(level)
+    p.postVelBlur, p.cgAccuracy, p.blurType = postVelBlur, cgAccuracy, int(blurType)
+    p.cfl, p.orderTime, p.orderSpace = cfl, int(orderTime), int(orderSpace)
+    p.resetBndWidth, p.multiStep = resetBndWidth, int(multiStep)
+    p.projSizeThresh, p.minGridSize = int(projSizeThresh), int(minGridSize)
+    p.doFinalProject, p.cgMaxIter = int(bool(doFinalProject)), int(cgMaxIter)
+    err = ctypes.c_float()
+    st = SolveStats()
+    ctx = _ctx_of(vel)
+    check(ctx.lib.flof_opticalFlowMultiscale4d(ctx.h, vel.h, i0.h, i1.h, ctypes.byref(p),
+                                               ctypes.byref(err), ctypes.byref(st)))
+    _last_stats = st.as_dict()
+    return float(err.value)
+
+
+def opticalFlow4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, postVelBlur=0.0, cgAccuracy=1e-04,
+                  blurType=1, resetBndWidth=-1.0, cgMaxIter=1000):
+    """opticalFlow4d (optflow4d.cpp:2110-2119); returns (iterations, residual)."""
+    ctx = _ctx_of(vel)
+    it = ctypes.c_int()
+    res = ctypes.c_float()
+    check(ctx.lib.flof_opticalFlow4d(ctx.h, vel.h, i0.h, i1.h, wSmooth, wEnergy, postVelBlur, cgAccuracy,
+                                     int(blurType), resetBndWidth, int(cgMaxIter), ctypes.byref(it),
+                                     ctypes.byref(res)))
+    return int(it.value), float(res.value)
+
+
+def corrVelsOf4d(dst, vel, phiOrg, phiCurr, phiTarget, threshPhi=1e10, threshNorm=1e10, postVelBlur=0.0,
+                 resetBndWidth=-1.0, maxIter=100):
+    """corrVelsOf4d (optflow4d.cpp:2121-2130)."""
+    ctx = _ctx_of(vel)
+    check(ctx.lib.flof_corrVelsOf4d(ctx.h, dst.h, vel.h, phiOrg.h, phiCurr.h if phiCurr is not None else None,
+                                    phiTarget.h, threshPhi, threshNorm, postVelBlur, resetBndWidth,
+                                    int(maxIter)))
+
+
+def gaussianBlur4d(grid, sigma, blurType=1):
+    """gaussianBlurGeneric (optflow4d.cpp:160-174) on a Real or Vec4 grid."""
+    ctx = _ctx_of(grid)
+    check(ctx.lib.flof_gaussianBlur4d(ctx.h, grid.h, float(sigma), int(blurType)))
+
+
+def advect4d(vel, grid, dtFac=1.0):
+    """advect4d (optflow4d.cpp:1292-1306)."""
+    ctx = _ctx_of(vel)
+    check(ctx.lib.flof_advect4d(ctx.h, vel.h, grid.h, dtFac))
+
+
+def calcLsDiff4d(i0, i1, out=None, correction=1.0, bnd=0):
+    """calcLsDiff4d (optflow4d.cpp:2132-2137)."""
+    ctx = _ctx_of(i0)
+    r = ctypes.c_float()
+    check(ctx.lib.flof_calcLsDiff4d(ctx.h, i0.h, i1.h, out.h if out is not None else None, correction,
+                                    int(bnd), ctypes.byref(r)))
+    return float(r.value)
+
+
+def interpolateGrid4d(target, source, offset=None, scale=None, size=None):
+    """interpolateGrid4d (grid4d.cpp:539-547)."""
+    ctx = _ctx_of(target)
+    check(ctx.lib.flof_interpolateGrid4d(ctx.h, target.h, source.h, f4(offset if offset is not None else 0.0),
+                                         f4(scale if scale is not None else 1.0),
+                                         f4(size if size is not None else -1.0)))
+
+
+def interpolateGrid4dVec(target, source, offset=None, scale=None, size=None):
+    """interpolateGrid4dVec (grid4d.cpp:549-557)."""
+    ctx = _ctx_of(target)
+    check(ctx.lib.flof_interpolateGrid4dVec(ctx.h, target.h, source.h,
+                                            f4(offset if offset is not None else 0.0),
+                                            f4(scale if scale is not None else 1.0),
+                                            f4(size if size is not None else -1.0)))
+
+
+def deform4d(out, i0, i1, vel, velInv=None, alpha=1.0, twoway=1):
+    """The mode-2 apply of scenes/flof.py deform4d (:591-615) in one call."""
+    ctx = _ctx_of(out)
+    alphaInv = float(np.float32(1.0 - alpha))
+    check(ctx.lib.flof_deform4d(ctx.h, out.h, i0.h, i1.h if i1 is not None else None, vel.h,
+                                velInv.h if velInv is not None else None, float(alpha), alphaInv,
+                                int(twoway)))
+
+
+def loadAdvectTimeSlice_OptInit(ID, fname1, useDefoVols=False, doAligned=False, partialLoadFac=0.2):
+    """loadAdvectTimeSlice_OptInit (optflow4d.cpp:1871-1913).  `fname1` is the
+    deformation as a GPU-resident Grid4Vec4 instead of a .uni file name."""
+    if not isinstance(fname1, Grid4Vec4):
+        raise FlofError(1, "loadAdvectTimeSlice_OptInit expects the deformation as a Grid4Vec4")
+    ctx = fname1.ctx
+    check(ctx.lib.flof_loadAdvectTimeSlice_OptInit(ctx.h, int(ID), fname1.h, int(bool(useDefoVols)),
+                                                   int(bool(doAligned)), float(partialLoadFac)))
+    _lats_ctx[int(ID)] = ctx
+
+
+_lats_ctx: dict = {}
+
+
+def loadAdvectTimeSlice_OptRun(ID, fname, dst, phi, time, blendAlpha, loadTimeScale, defoOffset, defoScale,
+                               defoFactor, overrideSize=None, overrideTimeOff=0.0, debugVel=None,
+                               debugVelT=None, zeroVel=False, thirdAlpha=0.0, bordSkip=1, fourthAlpha=0.0,
+                               defoAniFac=1.0):
+    """loadAdvectTimeSlice_OptRun (optflow4d.cpp:1951-2105); `fname` is
+    accepted for call compatibility and ignored (the deformation was bound
+    at OptInit)."""
+    ctx = dst.ctx
+    check(ctx.lib.flof_loadAdvectTimeSlice_OptRun(
+        ctx.h, int(ID), dst.h, phi.h, float(time), float(blendAlpha), float(loadTimeScale), f4(defoOffset),
+        f4(defoScale), f4(defoFactor), f4(overrideSize if overrideSize is not None else -1.0),
+        float(overrideTimeOff), int(bool(zeroVel)), float(thirdAlpha), int(bordSkip), float(fourthAlpha),
+        float(defoAniFac)))
+
+
+def loadAdvectTimeSlice_OptRunTwoway(ID0, ID1, dst, phi0, phi1, time, blendAlpha, loadTimeScale, defoOffset,
+                                     defoScale, defoFactor, overrideSize=None, overrideTimeOff=0.0, bordSkip=1,
+                                     defoAniFac=1.0):
+    """Both directions of a two-way frame and their blend
+    (scenes/flof.py:750-755) in one GPU pass."""
+    ctx = dst.ctx
+    alphaInv = float(np.float32(1.0 - blendAlpha))
+    check(ctx.lib.flof_loadAdvectTimeSlice_OptRunTwoway(
+        ctx.h, int(ID0), int(ID1), dst.h, phi0.h, phi1.h, float(time), float(blendAlpha), alphaInv,
+        float(loadTimeScale), f4(defoOffset), f4(defoScale), f4(defoFactor),
+        f4(overrideSize if overrideSize is not None else -1.0), float(overrideTimeOff), int(bordSkip),
+        float(defoAniFac)))
+
+
+def loadAdvectTimeSlice_Finish(ID):
+    """loadAdvectTimeSlice_Finish (optflow4d.cpp:1930-1950)."""
+    ctx = _lats_ctx.pop(int(ID), None)
+    if ctx is None:
+        return
+    check(ctx.lib.flof_loadAdvectTimeSlice_Finish(ctx.h, int(ID)))

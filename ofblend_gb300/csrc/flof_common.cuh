@@ -1,0 +1,318 @@
+// flof_common.cuh -- device-side building blocks shared by the FlOF kernels.
+//
+// Layout (reference source/grid4d.h:92-97): a 4D grid (X,Y,Z,T) is stored
+// x-fastest, idx = i + X*j + X*Y*k + X*Y*Z*t.  Real grids are float, Vec4
+// grids are float4 (interleaved x,y,z,t), 16-byte aligned.
+//
+// Arithmetic: every translation unit is compiled with -fmad=false so that
+// multiplies and adds are rounded separately, in the order written, like the
+// reference's x86 build; fused multiply-adds appear only where a kernel asks
+// for them explicitly (__fmaf_rn) and the reference has no bitwise claim.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace flof {
+
+typedef long long idx_t;
+
+struct Dims4 {
+  int x, y, z, t;
+  __host__ __device__ idx_t cells() const { return (idx_t)x * y * z * t; }
+  __host__ __device__ idx_t sz() const { return (idx_t)x * y; }
+  __host__ __device__ idx_t st() const { return (idx_t)x * y * z; }
+  __host__ __device__ idx_t index(int i, int j, int k, int l) const {
+    return (idx_t)i + (idx_t)x * j + (idx_t)x * y * k + (idx_t)x * y * z * l;
+  }
+};
+
+// Unsigned division by an invariant divisor with a multiply-high
+// (Granlund & Montgomery, PLDI 1994, "round-up" variant).  Valid for every
+// 32-bit dividend.
+struct FastDiv {
+  uint32_t d, m, l;
+  FastDiv() : d(1), m(0), l(0) {}
+  explicit FastDiv(uint32_t div) : d(div) {
+    l = 0;
+    while ((1ull << l) < div) ++l;
+    uint64_t mm = ((1ull << 32) * ((1ull << l) - div)) / div + 1;
+    m = (uint32_t)mm;
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    uint64_t hi = __umulhi(n, m);
+    return (uint32_t)((hi + n) >> l);
+  }
+};
+
+// Cell coordinates of a linear index over a box of extents (ex,ey,ez,*).
+struct BoxDecoder {
+  FastDiv fx, fy, fz;
+  int ox, oy, oz, ot;  // coordinate offsets added after decoding
+  uint32_t ex, ey, ez;
+  __device__ __forceinline__ void decode(uint32_t n, int &i, int &j, int &k,
+                                         int &l) const {
+    uint32_t q = fx.div(n);
+    i = (int)(n - q * ex) + ox;
+    uint32_t q2 = fy.div(q);
+    j = (int)(q - q2 * ey) + oy;
+    uint32_t q3 = fz.div(q2);
+    k = (int)(q2 - q3 * ez) + oz;
+    l = (int)q3 + ot;
+  }
+};
+
+inline BoxDecoder make_decoder(int ex, int ey, int ez, int ox, int oy, int oz,
+                               int ot) {
+  BoxDecoder b;
+  b.fx = FastDiv((uint32_t)ex);
+  b.fy = FastDiv((uint32_t)ey);
+  b.fz = FastDiv((uint32_t)ez);
+  b.ex = (uint32_t)ex;
+  b.ey = (uint32_t)ey;
+  b.ez = (uint32_t)ez;
+  b.ox = ox;
+  b.oy = oy;
+  b.oz = oz;
+  b.ot = ot;
+  return b;
+}
+
+__device__ __forceinline__ bool in_bounds(const Dims4 &d, int i, int j, int k,
+                                          int l, int b) {
+  return i >= b && j >= b && i < d.x - b && j < d.y - b && k >= b &&
+         k < d.z - b && l >= b && l < d.t - b;
+}
+
+// float -> int truncation (cvt.rzi.s32.f32: NaN gives 0, out of range
+// saturates); equal to the reference's (int) cast for all in-range values.
+__device__ __forceinline__ int trunc_i(float p) { return __float2int_rz(p); }
+
+// Weights and base index of a quadrilinear sample, the reference's
+// BUILD_INDEX_4D (source/util/vector4d.h:422-470).  `1. - s1` is evaluated
+// in double by the reference; for a float s1 that equals 1.0f - s1.
+struct IW4 {
+  idx_t idx;
+  float s0, s1, t0, t1, f0, f1, g0, g1;
+};
+
+__device__ __forceinline__ IW4 build_index4(const Dims4 &sz, float p0, float p1,
+                                            float p2, float p3) {
+  IW4 w;
+  const float px = p0 - 0.5f, py = p1 - 0.5f, pz = p2 - 0.5f, pt = p3 - 0.5f;
+  int xi = trunc_i(px), yi = trunc_i(py), zi = trunc_i(pz), ti = trunc_i(pt);
+  w.s1 = px - (float)xi;
+  w.s0 = 1.0f - w.s1;
+  w.t1 = py - (float)yi;
+  w.t0 = 1.0f - w.t1;
+  w.f1 = pz - (float)zi;
+  w.f0 = 1.0f - w.f1;
+  w.g1 = pt - (float)ti;
+  w.g0 = 1.0f - w.g1;
+  if (px < 0.f) { xi = 0; w.s0 = 1.f; w.s1 = 0.f; }
+  if (py < 0.f) { yi = 0; w.t0 = 1.f; w.t1 = 0.f; }
+  if (pz < 0.f) { zi = 0; w.f0 = 1.f; w.f1 = 0.f; }
+  if (pt < 0.f) { ti = 0; w.g0 = 1.f; w.g1 = 0.f; }
+  if (xi >= sz.x - 1) { xi = sz.x - 2; w.s0 = 0.f; w.s1 = 1.f; }
+  if (yi >= sz.y - 1) { yi = sz.y - 2; w.t0 = 0.f; w.t1 = 1.f; }
+  if (zi >= sz.z - 1) { zi = sz.z - 2; w.f0 = 0.f; w.f1 = 1.f; }
+  if (ti >= sz.t - 1) { ti = sz.t - 2; w.g0 = 0.f; w.g1 = 1.f; }
+  w.idx = sz.index(xi, yi, zi, ti);
+  return w;
+}
+
+// interpol4d sum order (vector4d.h:497-512): pairs along y, then x, z, t.
+template <class LD>
+__device__ __forceinline__ float interp4_sum(const IW4 &w, idx_t sX, idx_t sY,
+                                             idx_t sZ, idx_t sT, LD ld) {
+  const idx_t i = w.idx;
+  const float t0 = w.t0, t1 = w.t1, s0 = w.s0, s1 = w.s1, f0 = w.f0,
+              f1 = w.f1, g0 = w.g0, g1 = w.g1;
+  return (((ld(i) * t0 + ld(i + sY) * t1) * s0 +
+           (ld(i + sX) * t0 + ld(i + sX + sY) * t1) * s1) *
+              f0 +
+          ((ld(i + sZ) * t0 + ld(i + sY + sZ) * t1) * s0 +
+           (ld(i + sX + sZ) * t0 + ld(i + sX + sY + sZ) * t1) * s1) *
+              f1) *
+             g0 +
+         (((ld(i + sT) * t0 + ld(i + sT + sY) * t1) * s0 +
+           (ld(i + sT + sX) * t0 + ld(i + sT + sX + sY) * t1) * s1) *
+              f0 +
+          ((ld(i + sT + sZ) * t0 + ld(i + sT + sY + sZ) * t1) * s0 +
+           (ld(i + sT + sX + sZ) * t0 + ld(i + sT + sX + sY + sZ) * t1) * s1) *
+              f1) *
+             g1;
+}
+
+__device__ __forceinline__ float interp4_real(const float *__restrict__ data,
+                                              const Dims4 &sz, float p0,
+                                              float p1, float p2, float p3) {
+  IW4 w = build_index4(sz, p0, p1, p2, p3);
+  return interp4_sum(w, 1, sz.x, sz.sz(), sz.st(),
+                     [&](idx_t q) { return __ldg(data + q); });
+}
+
+__device__ __forceinline__ float4 interp4_vec(const float4 *__restrict__ data,
+                                              const Dims4 &sz, float p0,
+                                              float p1, float p2, float p3) {
+  IW4 w = build_index4(sz, p0, p1, p2, p3);
+  const idx_t sX = 1, sY = sz.x, sZ = sz.sz(), sT = sz.st();
+  // Load the 16 corners once, then evaluate the sum per component.
+  float4 c[16];
+  const idx_t i = w.idx;
+  c[0] = __ldg(data + i);
+  c[1] = __ldg(data + i + sY);
+  c[2] = __ldg(data + i + sX);
+  c[3] = __ldg(data + i + sX + sY);
+  c[4] = __ldg(data + i + sZ);
+  c[5] = __ldg(data + i + sY + sZ);
+  c[6] = __ldg(data + i + sX + sZ);
+  c[7] = __ldg(data + i + sX + sY + sZ);
+  c[8] = __ldg(data + i + sT);
+  c[9] = __ldg(data + i + sT + sY);
+  c[10] = __ldg(data + i + sT + sX);
+  c[11] = __ldg(data + i + sT + sX + sY);
+  c[12] = __ldg(data + i + sT + sZ);
+  c[13] = __ldg(data + i + sT + sY + sZ);
+  c[14] = __ldg(data + i + sT + sX + sZ);
+  c[15] = __ldg(data + i + sT + sX + sY + sZ);
+  const float t0 = w.t0, t1 = w.t1, s0 = w.s0, s1 = w.s1, f0 = w.f0,
+              f1 = w.f1, g0 = w.g0, g1 = w.g1;
+#define FLOF_IP4(C)                                                            \
+  ((((c[0].C * t0 + c[1].C * t1) * s0 + (c[2].C * t0 + c[3].C * t1) * s1) *   \
+        f0 +                                                                   \
+    ((c[4].C * t0 + c[5].C * t1) * s0 + (c[6].C * t0 + c[7].C * t1) * s1) *   \
+        f1) *                                                                  \
+       g0 +                                                                    \
+   (((c[8].C * t0 + c[9].C * t1) * s0 + (c[10].C * t0 + c[11].C * t1) * s1) * \
+        f0 +                                                                   \
+    ((c[12].C * t0 + c[13].C * t1) * s0 +                                      \
+     (c[14].C * t0 + c[15].C * t1) * s1) *                                     \
+        f1) *                                                                  \
+       g1)
+  float4 r;
+  r.x = FLOF_IP4(x);
+  r.y = FLOF_IP4(y);
+  r.z = FLOF_IP4(z);
+  r.w = FLOF_IP4(w);
+#undef FLOF_IP4
+  return r;
+}
+
+// Trilinear Vec4 sample of a 3D field (interpol<T>, source/util/interpol.h
+// :57-116): z is clamped only when size.z > 1.
+__device__ __forceinline__ float4 interp3_vec(const float4 *__restrict__ data,
+                                              int sx, int sy, int sz, float q0,
+                                              float q1, float q2) {
+  const float px = q0 - 0.5f, py = q1 - 0.5f, pz = q2 - 0.5f;
+  int xi = trunc_i(px), yi = trunc_i(py), zi = trunc_i(pz);
+  float s1 = px - (float)xi, s0 = 1.0f - s1;
+  float t1 = py - (float)yi, t0 = 1.0f - t1;
+  float f1 = pz - (float)zi, f0 = 1.0f - f1;
+  if (px < 0.f) { xi = 0; s0 = 1.f; s1 = 0.f; }
+  if (py < 0.f) { yi = 0; t0 = 1.f; t1 = 0.f; }
+  if (pz < 0.f) { zi = 0; f0 = 1.f; f1 = 0.f; }
+  if (xi >= sx - 1) { xi = sx - 2; s0 = 0.f; s1 = 1.f; }
+  if (yi >= sy - 1) { yi = sy - 2; t0 = 0.f; t1 = 1.f; }
+  if (sz > 1) {
+    if (zi >= sz - 1) { zi = sz - 2; f0 = 0.f; f1 = 1.f; }
+  }
+  const idx_t X = 1, Y = sx, Z = (idx_t)sx * sy;
+  const idx_t i = (idx_t)xi + Y * yi + Z * zi;
+  float4 c[8];
+  c[0] = __ldg(data + i);
+  c[1] = __ldg(data + i + Y);
+  c[2] = __ldg(data + i + X);
+  c[3] = __ldg(data + i + X + Y);
+  c[4] = __ldg(data + i + Z);
+  c[5] = __ldg(data + i + Y + Z);
+  c[6] = __ldg(data + i + X + Z);
+  c[7] = __ldg(data + i + X + Y + Z);
+#define FLOF_IP3(C)                                                           \
+  (((c[0].C * t0 + c[1].C * t1) * s0 + (c[2].C * t0 + c[3].C * t1) * s1) *   \
+       f0 +                                                                   \
+   ((c[4].C * t0 + c[5].C * t1) * s0 + (c[6].C * t0 + c[7].C * t1) * s1) *   \
+       f1)
+  float4 r;
+  r.x = FLOF_IP3(x);
+  r.y = FLOF_IP3(y);
+  r.z = FLOF_IP3(z);
+  r.w = FLOF_IP3(w);
+#undef FLOF_IP3
+  return r;
+}
+
+// ---- reductions -----------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_min(float v) {
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum in a fixed tree order; the result is valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < NT / 32) ? sh[l] : 0.0;
+    v = warp_sum(v);
+  }
+  __syncthreads();
+  return v;
+}
+template <int NT>
+__device__ __forceinline__ float block_max(float v, float *sh) {
+  v = warp_max(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < NT / 32) ? sh[l] : -INFINITY;
+    v = warp_max(v);
+  }
+  __syncthreads();
+  return v;
+}
+template <int NT>
+__device__ __forceinline__ float block_min(float v, float *sh) {
+  v = warp_min(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = (l < NT / 32) ? sh[l] : INFINITY;
+    v = warp_min(v);
+  }
+  __syncthreads();
+  return v;
+}
+
+// "Last block" completion: every block has published its partial result
+// before it increments the counter; the block that sees gridDim.x-1 combines
+// the partials in index order (deterministic) and resets the counter.  No
+// block ever waits on another.
+__device__ __forceinline__ bool last_block_arrives(unsigned int *counter) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int prev = atomicAdd(counter, 1u);
+    is_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+}  // namespace flof

@@ -1,0 +1,1499 @@
+// flof_host.cu -- context, device grid pool, the FlOF multiscale driver and
+// the C ABI declared in include/flof_gb300.h.
+//
+// The driver restates the control flow of the reference
+// (source/plugin/optflow4d.cpp): opticalFlowMultiscaleTemplate :936-1173,
+// opticalFlowDim :361-553, corrVelsOfTempl :737-802, gaussianBlurGeneric
+// :160-174, advectCflHelper4d :1309-1321, loadAdvectTimeSlice_OptRun
+// :1951-2105.  All data stays in device memory; the host only decides the
+// data-dependent control (CG convergence, multistep stop rule, CFL substeps,
+// extrapolation sweep count), reading those scalars back on the context
+// stream.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <chrono>
+#include <map>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/flof_gb300.h"
+#include "flof_kernels.h"
+
+using namespace flof;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct FlofError {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw FlofError{code, msg}; }
+
+void cuda_check(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return;
+  const int code = (e == cudaErrorMemoryAllocation) ? FLOF_E_OOM : FLOF_E_CUDA;
+  fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CK(call) cuda_check((call), #call)
+
+struct Pool {
+  std::unordered_map<size_t, std::vector<void *>> free_list;
+  std::unordered_map<void *, size_t> owned;
+  size_t bytes = 0;
+
+  void *get(size_t n) {
+    if (n == 0) n = 16;
+    n = (n + 255) & ~size_t(255);
+    auto it = free_list.find(n);
+    if (it != free_list.end() && !it->second.empty()) {
+      void *p = it->second.back();
+      it->second.pop_back();
+      return p;
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      trim();
+      e = cudaMalloc(&p, n);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        fail(FLOF_E_OOM, "device allocation of " + std::to_string(n) + " bytes failed");
+      }
+    }
+    owned[p] = n;
+    bytes += n;
+    return p;
+  }
+  void put(void *p) {
+    if (!p) return;
+    auto it = owned.find(p);
+    if (it == owned.end()) return;
+    free_list[it->second].push_back(p);
+  }
+  void trim() {
+    for (auto &kv : free_list) {
+      for (void *p : kv.second) {
+        cudaFree(p);
+        owned.erase(p);
+        bytes -= kv.first;
+      }
+      kv.second.clear();
+    }
+  }
+  void release_all() {
+    for (auto &kv : owned) cudaFree(kv.first);
+    owned.clear();
+    free_list.clear();
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+enum KClass {
+  KC_OTHER = 0, KC_ASSEMBLE, KC_MATVEC, KC_UPDATE, KC_DIRECTION, KC_COPYBACK, KC_BLUR,
+  KC_PROJECT, KC_EXPOL, KC_ADVECT, KC_RESAMPLE, KC_LSDIFF, KC_REDUCE, KC_ELEMWISE, KC_BORDER,
+  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_COUNT
+};
+static const char *kc_names[KC_COUNT] = {
+    "other", "of_assemble_init", "cg_matvec", "cg_update", "cg_direction", "of_copy_back",
+    "gauss_blur", "project_cells", "expol_sweep", "advect", "resample", "ls_diff", "reduce",
+    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices"};
+
+struct ProfRec {
+  int cls;
+  int size_x;
+  double bytes;
+  cudaEvent_t e0, e1;
+};
+
+struct LatsData {
+  const flof_grid *defo = nullptr;
+  void *vt = nullptr;  // blended t-slice (Vec4, X*Y*Z of the defo)
+  int lastT = -1;
+};
+
+struct flof_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  Pool pool;
+  CGState *st = nullptr;    // device
+  CGState *st_h = nullptr;  // pinned host mirror
+  double *dpart = nullptr;
+  float *fpart = nullptr;
+  unsigned int *counter = nullptr;  // 8 zeroed counters
+  float *fres = nullptr;            // 16 device scalars
+  double *dres = nullptr;
+  float *fres_h = nullptr;          // pinned
+  double *dres_h = nullptr;
+  long long launches = 0;
+  int syncs = 0;
+  std::map<int, LatsData> lats;
+  flof_solve_stats *stats = nullptr;
+  int cfl_sync = 1;
+  int profiling = 0;
+  std::vector<ProfRec> recs;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+};
+
+struct flof_grid {
+  flof_ctx *ctx = nullptr;
+  int dims[4] = {0, 0, 0, 0};
+  int elem = FLOF_REAL;
+  void *d = nullptr;
+  bool owned = false;
+  Dims4 D() const { return Dims4{dims[0], dims[1], dims[2], dims[3]}; }
+  int nc() const { return elem == FLOF_VEC4 ? 4 : 1; }
+  long long cells() const { return (long long)dims[0] * dims[1] * dims[2] * dims[3]; }
+  size_t bytes() const { return (size_t)cells() * nc() * sizeof(float); }
+  float *f() const { return (float *)d; }
+  float4 *v() const { return (float4 *)d; }
+};
+
+namespace {
+
+// RAII device buffer from the context pool.
+struct DBuf {
+  flof_ctx *c = nullptr;
+  void *p = nullptr;
+  DBuf() {}
+  DBuf(flof_ctx *ctx, size_t n) : c(ctx), p(ctx->pool.get(n)) {}
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : c(o.c), p(o.p) { o.p = nullptr; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      c = o.c;
+      p = o.p;
+      o.p = nullptr;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release() {
+    if (p && c) c->pool.put(p);
+    p = nullptr;
+  }
+  float *f() const { return (float *)p; }
+  float4 *v() const { return (float4 *)p; }
+};
+
+inline size_t real_bytes(Dims4 d) { return (size_t)d.cells() * sizeof(float); }
+inline size_t vec_bytes(Dims4 d) { return (size_t)d.cells() * sizeof(float4); }
+
+// Kernel launch with optional event tracing: when the context profiles,
+// every launch is bracketed by two CUDA events on the context stream and
+// recorded with its kernel class, the X extent of its grid and its
+// algorithmic bytes (compulsory reads + writes).
+#define KLP(ctx, cls, sx, nbytes, call)                                   \
+  do {                                                                     \
+    flof_ctx *_c = (ctx);                                                  \
+    cudaEvent_t _e0 = nullptr, _e1 = nullptr;                              \
+    if (_c->profiling) {                                                   \
+      _e0 = prof_event(_c);                                                \
+      _e1 = prof_event(_c);                                                \
+      CK(cudaEventRecord(_e0, _c->stream));                                \
+    }                                                                      \
+    call;                                                                  \
+    ++_c->launches;                                                        \
+    if (_c->profiling) {                                                   \
+      CK(cudaEventRecord(_e1, _c->stream));                                \
+      _c->recs.push_back(ProfRec{(cls), (sx), (double)(nbytes), _e0, _e1}); \
+    }                                                                      \
+  } while (0)
+#define KL(ctx, call) KLP(ctx, KC_OTHER, 0, 0, call)
+
+inline long long nint(Dims4 d) {
+  if (d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3) return 0;
+  return (long long)(d.x - 2) * (d.y - 2) * (d.z - 2) * (d.t - 2);
+}
+
+cudaEvent_t prof_event(flof_ctx *c) {
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->ev_pool.push_back(e);
+  }
+  return c->ev_pool[c->ev_used++];
+}
+
+void sync(flof_ctx *c) {
+  CK(cudaStreamSynchronize(c->stream));
+  c->syncs++;
+}
+
+float read_f(flof_ctx *c, const float *dev) {
+  CK(cudaMemcpyAsync(c->fres_h, dev, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  return c->fres_h[0];
+}
+
+int trunc_f(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.f) return 2147483647;
+  if (v <= -2147483648.f) return (-2147483647 - 1);
+  return (int)v;
+}
+int trunc_d(double v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.0) return 2147483647;
+  if (v <= -2147483648.0) return (-2147483647 - 1);
+  return (int)v;
+}
+
+void record_solve(flof_ctx *c, int sx, int iters, float res, int status) {
+  flof_solve_stats *s = c->stats;
+  if (!s) return;
+  if (s->nsolves < FLOF_MAX_SOLVE_STATS) {
+    s->size_x[s->nsolves] = sx;
+    s->iterations[s->nsolves] = iters;
+    s->residual[s->nsolves] = res;
+    s->status[s->nsolves] = status;
+  }
+  s->nsolves++;
+  s->cg_total_iterations += iters > 0 ? iters : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Building blocks of the driver
+// ---------------------------------------------------------------------------
+
+// interpolGridTempl (optflow4d.cpp:40-57): factor = Real(src)/target per
+// axis, offset = factor * 0.5.
+void interpol_grid(flof_ctx *c, float *target, Dims4 td, const float *source, Dims4 sd,
+                   int nc) {
+  const int sa[4] = {sd.x, sd.y, sd.z, sd.t}, ta[4] = {td.x, td.y, td.z, td.t};
+  float fac[4], off[4];
+  for (int q = 0; q < 4; ++q) {
+    fac[q] = (float)sa[q] / (float)ta[q];
+    off[q] = (float)((double)fac[q] * 0.5);
+  }
+  KLP(c, KC_RESAMPLE, td.x, (td.cells() + sd.cells()) * nc * 4,
+      launch_resample(target, td, source, sd, nc, make_float4(fac[0], fac[1], fac[2], fac[3]),
+                        make_float4(off[0], off[1], off[2], off[3]), c->stream));
+}
+
+// max |v| of a Vec4 grid (getMaxValue, grid4d.cpp:274-277), synchronising.
+float vec_max_norm(flof_ctx *c, const float4 *v, Dims4 d) {
+  KLP(c, KC_REDUCE, d.x, d.cells() * 16,
+      launch_reduce_minmax((const float *)v, d.cells(), 4, 0, c->fpart, c->counter + 4,
+                             c->fres + 0, c->stream));
+  const float m2 = read_f(c, c->fres + 0);
+  return sqrtf(m2);
+}
+
+// advectCflTemplate<Grid4d<int>,...> (optflow4d.cpp:2170-2180) ->
+// advectCflHelper4d (:1309-1321) with the solver dt = 1 and velFactor = 1
+// (a multiplication by 1 is exact, so the velocity copy is skipped).
+void advect_cfl(flof_ctx *c, Dims4 d, float cfl, const float4 *vel, float *grid, int nc) {
+  const float orgDt = 1.0f;
+  const float maxVel = vec_max_norm(c, vel, d) * orgDt;
+  const int steps = trunc_f(maxVel / cfl) + 1;
+  if (steps < 1 || steps > (1 << 16))
+    fail(FLOF_E_NAN, "CFL substep count out of range (non-finite or huge velocities)");
+  const float mdt = orgDt / (float)steps;
+  DBuf tmp(c, (size_t)d.cells() * nc * sizeof(float));
+  float *a = grid, *b = tmp.f();
+  for (int s = 0; s < steps; ++s) {
+    KLP(c, KC_ADVECT, d.x, d.cells() * (16 + 8 * nc),
+        launch_advect(vel, a, b, d, nc, mdt * 1.0f, c->stream));
+    float *sw = a;
+    a = b;
+    b = sw;
+  }
+  if (a != grid)
+    CK(cudaMemcpyAsync(grid, a, (size_t)d.cells() * nc * sizeof(float),
+                       cudaMemcpyDeviceToDevice, c->stream));
+}
+
+// calcLsDiffTempl (optflow4d.cpp:895-927), synchronising.
+float ls_diff(flof_ctx *c, const float *i0, const float *i1, float *out, Dims4 d, float corr,
+              int bnd) {
+  KLP(c, KC_LSDIFF, d.x, d.cells() * 8,
+      launch_ls_diff(i0, i1, out, d, corr, bnd, c->dpart, c->counter + 5, c->dres + 0,
+                       c->fres + 1, c->stream));
+  return read_f(c, c->fres + 1);
+}
+
+// gaussianBlurGeneric(a, sigma, iter = 1) (optflow4d.cpp:160-174).
+void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurType) {
+  int s = trunc_d(1. * (double)sigma + 0.5);
+  if (s == 0) s = 1;
+  if (s > 6 || s < 0) fail(FLOF_E_ARG, "Gaussian blur radius above 6 cells is not supported");
+  const size_t nb = (size_t)d.cells() * nc * sizeof(float);
+  if (blurType != FLOF_BLUR_GAUSS_SEPARABLE) {
+    float wtab[160];
+    for (int q = 0; q <= 4 * s * s; ++q)
+      wtab[q] = (float)exp((double)(-(float)q) / (2. * (double)sigma * (double)sigma));
+    DBuf tmp(c, nb);
+    // pass 1: a -> fresh tmp (zero ring); pass 2: tmp -> a (ring keeps the
+    // original values): the state after the reference's two swaps.
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_pass(a, tmp.f(), d, nc, s, wtab, 1, c->stream));
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_pass(tmp.f(), a, d, nc, s, wtab, 0, c->stream));
+  } else {
+    float w1[8];
+    for (int q = 0; q <= s; ++q)
+      w1[q] = (float)exp((double)(-(float)(q * q)) / (2. * (double)sigma * (double)sigma));
+    DBuf t1(c, nb), t2(c, nb), t3(c, nb);
+    KL(c, launch_gauss_sep_pass(a, t1.f(), d, nc, 0, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t1.f(), t2.f(), d, nc, 1, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t2.f(), t1.f(), d, nc, 2, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t1.f(), t3.f(), d, nc, 3, s, w1, 1, c->stream));
+    KL(c, launch_gauss_sep_pass(t3.f(), t1.f(), d, nc, 0, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t1.f(), t2.f(), d, nc, 1, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t2.f(), t1.f(), d, nc, 2, s, w1, 0, c->stream));
+    KL(c, launch_gauss_sep_pass(t1.f(), a, d, nc, 3, s, w1, 2, c->stream));
+  }
+}
+
+struct OFArgs {
+  float wSmooth, wEnergy, postVelBlur, cgAccuracy, resetBndWidth;
+  int blurType, cgMaxIter;
+};
+
+// opticalFlowDim<Grid4d<Real>,Grid4d<Vec4>,4> (optflow4d.cpp:361-553).
+// velIn (nullable) is the input velocity used in the rhs; the result goes
+// to velOut (may alias velIn).
+void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
+                      const float *i0w, const float *i1, const OFArgs &a, int *itersOut,
+                      float *resOut) {
+  const size_t vb = vec_bytes(d);
+  DBuf g(c, vb), r(c, vb), p(c, vb), q(c, vb), x(c, vb);
+  OFConsts k;
+  k.mDx = (float)(1. / d.x);
+  k.mDt = 1.0f;
+  k.dxf = (float)(1. / (2. * (double)k.mDx));
+  k.wSmooth = a.wSmooth;
+  k.wEnergy = a.wEnergy;
+  k.offd = -a.wSmooth * 1.0f;
+  float diag = 0.f;
+  diag += (float)(2 * 4) * a.wSmooth * 1.0f;
+  diag += a.wEnergy;
+  k.diag = diag;
+
+  KLP(c, KC_ASSEMBLE, d.x, nint(d) * 8 + d.cells() * 64,
+      launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
+                                a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
+  int it = 0;
+  int chunk = 4;
+  for (;;) {
+    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (c->st_h->done != CG_RUNNING) break;
+    if (it >= a.cgMaxIter) break;
+    // Estimate the remaining iterations from the observed reduction rate.
+    if (it > 0) {
+      const double ratio = (double)c->st_h->resMax / c->st_h->resIni;
+      const double target = c->st_h->acc / c->st_h->resIni;
+      if (ratio > 0 && ratio < 1 && target > 0) {
+        const double rate = log(ratio) / it;
+        double est = rate < 0 ? (log(target) - log(ratio)) / rate : 64;
+        int e = (int)(est * 1.1) + 2;
+        chunk = e < 2 ? 2 : (e > 64 ? 64 : e);
+      } else {
+        chunk = chunk * 2 > 64 ? 64 : chunk * 2;
+      }
+    }
+    const int n = (a.cgMaxIter - it) < chunk ? (a.cgMaxIter - it) : chunk;
+    for (int s = 0; s < n; ++s) {
+      KLP(c, KC_MATVEC, d.x, nint(d) * 48,
+          launch_cg_matvec(p.v(), g.v(), q.v(), d, k, c->st, c->dpart, c->stream));
+      KLP(c, KC_UPDATE, d.x, nint(d) * 112,
+          launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, c->st, c->dpart,
+                             c->fpart, it + s, a.cgMaxIter, c->stream));
+      KLP(c, KC_DIRECTION, d.x, nint(d) * 64,
+          launch_cg_direction(p.v(), r.v(), g.v(), d, k, c->st, c->stream));
+    }
+    it += n;
+  }
+  int status = c->st_h->done;
+  if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
+  const int iters = c->st_h->iters;
+  const float res = c->st_h->retResidual;
+  record_solve(c, d.x, iters, res, status);
+  if (itersOut) *itersOut = iters;
+  if (resOut) *resOut = res;
+
+  KLP(c, KC_COPYBACK, d.x, d.cells() * 32,
+      launch_of_copy_back(x.v(), velOut, d.cells(), k.mDx, c->st, c->stream));
+  if (a.postVelBlur > 0.f) {
+    if (a.blurType != 1 && a.blurType != FLOF_BLUR_GAUSS_SEPARABLE)
+      fail(FLOF_E_ARG, "blurType must be 1 (Gaussian) or 2 (separable Gaussian)");
+    gauss_blur(c, (float *)velOut, d, 4, (float)(0.5 * a.postVelBlur), a.blurType);
+  }
+  if (a.resetBndWidth > 0.f) {
+    const int rb = trunc_f(a.resetBndWidth * (float)d.x) + 1;
+    KLP(c, KC_BORDER, d.x, 0, launch_reset_outside(velOut, d, rb, c->stream));
+  }
+}
+
+// corrVelsOfTempl (optflow4d.cpp:737-802).  dst receives the correction of
+// the last round; vel is corrected in place.
+void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *phiOrg,
+                  const float *phiTarget, float threshPhi, float postVelBlur,
+                  float resetBndWidth, int maxIter, int blurType) {
+  const float blurThreshold = 0.98f;
+  const int doCvExtrapol = trunc_f(vec_max_norm(c, vel, d) + 4);
+  if (doCvExtrapol > (1 << 16))
+    fail(FLOF_E_NAN, "extrapolation sweep count out of range (non-finite or huge velocities)");
+  if (!(postVelBlur < 1e30f) && postVelBlur == postVelBlur)
+    fail(FLOF_E_ARG, "postVelBlur must be finite");
+  DBuf marker(c, real_bytes(d)), tmp(c, vec_bytes(d));
+  int singleStep = 0;
+  if (postVelBlur < blurThreshold) singleStep = 1;
+  float4 *A = dst;
+  while ((postVelBlur >= blurThreshold) || singleStep) {
+    A = dst;
+    float4 *B = tmp.v();
+    CK(cudaMemsetAsync(dst, 0, vec_bytes(d), c->stream));
+    CK(cudaMemsetAsync(marker.p, 0, real_bytes(d), c->stream));
+    KLP(c, KC_PROJECT, d.x, d.cells() * 44,
+        launch_project_cells(dst, vel, phiOrg, phiTarget, marker.f(), d, threshPhi, maxIter,
+                               c->stream));
+    for (int s = 0; s < doCvExtrapol; ++s) {
+      KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_sweep(A, B, marker.f(), d, c->stream));
+      float4 *sw = A;
+      A = B;
+      B = sw;
+    }
+    if (postVelBlur > 1e-6f) gauss_blur(c, (float *)A, d, 4, (float)(0.5 * postVelBlur), blurType);
+    const int resetBnd = trunc_f(resetBndWidth * (float)d.x) + 1;
+    if (resetBndWidth > 0.f)
+      KLP(c, KC_BORDER, d.x, 0,
+          launch_set_bound((float *)A, d, 4, make_float4(0.f, 0.f, 0.f, 0.f), resetBnd,
+                             c->stream));
+    KLP(c, KC_ELEMWISE, d.x, d.cells() * 48,
+        launch_add_scaled((float *)vel, (const float *)A, d.cells(), 4,
+                            make_float4(-1.f, -1.f, -1.f, -1.f), c->stream));
+    postVelBlur = (float)((double)postVelBlur * 0.5);
+    if (singleStep > 0) singleStep--;
+    if (A != dst) {
+      // keep the round's correction in dst (the reference swaps pointers)
+      CK(cudaMemcpyAsync(dst, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+      A = dst;
+    }
+  }
+}
+
+struct MSArgs {
+  float wSmooth, wEnergy, postVelBlur, cgAccuracy, cfl, resetBndWidth;
+  int blurType, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter;
+};
+
+// opticalFlowMultiscaleTemplate (optflow4d.cpp:936-1173).
+float multiscale(flof_ctx *c, Dims4 d, float4 *vel, const float *i0, const float *i1,
+                 const MSArgs &p, int level) {
+  const long long n4 = d.cells() * 4;
+  const int resetBnd = p.resetBndWidth > 0 ? trunc_f(p.resetBndWidth * (float)d.x) + 1 : 0;
+  const float projMaxDist = 4.f;
+  const int projMaxIter = 40;
+  const float lsDiffFac = (float)(0.1 / 20.);
+  OFArgs oa;
+  oa.wSmooth = p.wSmooth;
+  oa.wEnergy = p.wEnergy;
+  oa.cgAccuracy = p.cgAccuracy;
+  oa.resetBndWidth = p.resetBndWidth;
+  oa.blurType = p.blurType;
+  oa.cgMaxIter = p.cgMaxIter;
+
+  DBuf i0warped(c, real_bytes(d));
+  CK(cudaMemcpyAsync(i0warped.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+
+  if (d.x > p.minGridSize) {
+    Dims4 sd{d.x / 2, d.y / 2, d.z / 2, d.t / 2};
+    DBuf velSm(c, vec_bytes(sd)), i0Sm(c, real_bytes(sd)), i1Sm(c, real_bytes(sd));
+    interpol_grid(c, i0Sm.f(), sd, i0, d, 1);
+    interpol_grid(c, i1Sm.f(), sd, i1, d, 1);
+    interpol_grid(c, velSm.f(), sd, (const float *)vel, d, 4);
+    KL(c, launch_mult_const(velSm.f(), sd.cells(), 4, make_float4(0.5f, 0.5f, 0.5f, 0.5f),
+                            c->stream));
+    multiscale(c, sd, velSm.v(), i0Sm.f(), i1Sm.f(), p, level + 1);
+    interpol_grid(c, (float *)vel, d, velSm.f(), sd, 4);
+    KL(c, launch_mult_const((float *)vel, d.cells(), 4, make_float4(2.f, 2.f, 2.f, 2.f),
+                            c->stream));
+  }
+
+  advect_cfl(c, d, p.cfl, vel, i0warped.f(), 1);
+  KLP(c, KC_BORDER, d.x, 0, launch_set_bound_neumann(i0warped.f(), d, 1, 0, c->stream));
+  float errCurr = ls_diff(c, i0warped.f(), i1, nullptr, d, lsDiffFac, resetBnd);
+
+  bool doProject = false;
+  int multiStep = p.multiStep;
+  int doFinalProject = p.doFinalProject;
+  if (d.x > p.projSizeThresh) {
+    doProject = true;
+    multiStep = 1;
+    if (doFinalProject) doFinalProject = 0;
+  }
+  if (multiStep >= 10) fail(FLOF_E_ARG, "Too many of substeps!");
+
+  if (multiStep > 1) {
+    std::vector<DBuf> vs(multiStep), vs2(multiStep);
+    for (int of = 0; of < multiStep; ++of) vs2[of] = DBuf(c, vec_bytes(d));
+    DBuf tmpVel(c, vec_bytes(d)), i0warp2(c, real_bytes(d));
+    float velBlur = p.postVelBlur;
+    float errLast = errCurr;
+    int ofStepsCurr = multiStep;
+    for (int of = 0; of < ofStepsCurr; ++of) {
+      vs[of] = DBuf(c, vec_bytes(d));
+      oa.postVelBlur = velBlur;
+      // a fresh zero grid: its rhs terms in vel vanish, so velIn = null
+      optical_flow_dim(c, d, vs[of].v(), nullptr, i0warped.f(), i1, oa, nullptr, nullptr);
+      velBlur = (float)((double)velBlur * (3. / 4.));
+      if (velBlur < 2.f) velBlur = 2.f;
+      for (int k = of; k >= 0; --k)
+        CK(cudaMemcpyAsync(vs2[k].p, vs[k].p, vec_bytes(d), cudaMemcpyDeviceToDevice,
+                           c->stream));
+      for (int k = of - 1; k >= 0; --k)
+        for (int l = 0; l < k; ++l) advect_cfl(c, d, p.cfl, vs2[k].v(), vs2[l].f(), 4);
+      CK(cudaMemcpyAsync(tmpVel.p, vel, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+      for (int k = of; k >= 0; --k)
+        KLP(c, KC_ELEMWISE, d.x, n4 * 12, launch_add(tmpVel.f(), vs2[k].f(), n4, c->stream));
+      CK(cudaMemcpyAsync(i0warp2.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+      advect_cfl(c, d, p.cfl, tmpVel.v(), i0warp2.f(), 1);
+      KLP(c, KC_BORDER, d.x, 0, launch_set_bound_neumann(i0warp2.f(), d, 1, 0, c->stream));
+      const float errC = ls_diff(c, i0warp2.f(), i1, nullptr, d, lsDiffFac, resetBnd);
+      CK(cudaMemcpyAsync(i0warped.p, i0warp2.p, real_bytes(d), cudaMemcpyDeviceToDevice,
+                         c->stream));
+      if (of > 0 && (double)(errC / errLast) > 0.95) {
+        CK(cudaMemsetAsync(vs[of].p, 0, vec_bytes(d), c->stream));
+        ofStepsCurr = of + 1;
+      }
+      errLast = errC;
+    }
+    for (int of = ofStepsCurr - 1; of >= 0; --of)
+      for (int l = 0; l < of; ++l) advect_cfl(c, d, p.cfl, vs[of].v(), vs[l].f(), 4);
+    for (int of = 0; of < ofStepsCurr; ++of)
+      KLP(c, KC_ELEMWISE, d.x, n4 * 12, launch_add((float *)vel, vs[of].f(), n4, c->stream));
+  } else {
+    DBuf velCurr(c, vec_bytes(d));
+    if (!doProject) {
+      oa.postVelBlur = p.postVelBlur;
+      optical_flow_dim(c, d, velCurr.v(), nullptr, i0warped.f(), i1, oa, nullptr, nullptr);
+      KL(c, launch_add((float *)vel, velCurr.f(), n4, c->stream));
+    } else {
+      DBuf velTmp2(c, vec_bytes(d));
+      CK(cudaMemsetAsync(velTmp2.p, 0, vec_bytes(d), c->stream));
+      corr_vels_of(c, d, velCurr.v(), velTmp2.v(), i0warped.f(), i1, projMaxDist,
+                   p.postVelBlur, p.resetBndWidth, projMaxIter, p.blurType);
+      KL(c, launch_add((float *)vel, velTmp2.f(), n4, c->stream));
+      KL(c, launch_mult_const(velCurr.f(), d.cells(), 4, make_float4(-1.f, -1.f, -1.f, -1.f),
+                              c->stream));
+      KL(c, launch_add((float *)vel, velCurr.f(), n4, c->stream));
+    }
+  }
+
+  if (level == 0 && doFinalProject) {
+    DBuf velCurr(c, vec_bytes(d));
+    const float finalProjBlur = 4.f;
+    corr_vels_of(c, d, velCurr.v(), vel, i0, i1, projMaxDist, finalProjBlur, p.resetBndWidth,
+                 projMaxIter, p.blurType);
+  }
+
+  if (level == 0) {
+    CK(cudaMemcpyAsync(i0warped.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+    advect_cfl(c, d, p.cfl, vel, i0warped.f(), 1);
+    KLP(c, KC_BORDER, d.x, 0, launch_set_bound_neumann(i0warped.f(), d, 1, 0, c->stream));
+    errCurr = ls_diff(c, i0warped.f(), i1, nullptr, d, lsDiffFac, resetBnd);
+  }
+  return errCurr;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI helpers
+// ---------------------------------------------------------------------------
+
+template <class F>
+int guarded(F &&f) {
+  try {
+    f();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) fail(FLOF_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return FLOF_OK;
+  } catch (const FlofError &e) {
+    g_last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return FLOF_E_OOM;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return FLOF_E_CUDA;
+  }
+}
+
+void need(bool cond, const std::string &msg) {
+  if (!cond) fail(FLOF_E_ARG, msg);
+}
+void need_grid(const flof_grid *g, const char *name) {
+  need(g != nullptr, std::string(name) + " is NULL");
+  need(g->d != nullptr || g->cells() == 0, std::string(name) + " has no storage");
+}
+void same_size(const flof_grid *a, const flof_grid *b, const char *what) {
+  need(a->dims[0] == b->dims[0] && a->dims[1] == b->dims[1] && a->dims[2] == b->dims[2] &&
+           a->dims[3] == b->dims[3],
+       std::string(what) + ": different grid resolutions");
+}
+void need_elem(const flof_grid *g, int elem, const char *name) {
+  need(g->elem == elem, std::string(name) + (elem == FLOF_VEC4 ? " must be a Vec4 grid"
+                                                               : " must be a Real grid"));
+}
+void need_4d(const flof_grid *g, const char *name) {
+  for (int q = 0; q < 4; ++q)
+    need(g->dims[q] >= 2, std::string(name) + ": every extent must be at least 2");
+}
+void set_ctx_device(flof_ctx *c) { CK(cudaSetDevice(c->device)); }
+
+float4 f4(const float *v, int nc) {
+  if (!v) return make_float4(0.f, 0.f, 0.f, 0.f);
+  if (nc == 1) return make_float4(v[0], v[0], v[0], v[0]);
+  return make_float4(v[0], v[1], v[2], v[3]);
+}
+
+// gridFactor4d (grid4d.cpp:559-569)
+void grid_factor4d(const float s1[4], const float s2in[4], const float optSize[4],
+                   const float scale[4], float srcFac[4], float retOff[4]) {
+  float s2[4];
+  for (int q = 0; q < 4; ++q) s2[q] = optSize[q] > 0.f ? optSize[q] : s2in[q];
+  for (int q = 0; q < 4; ++q) srcFac[q] = (s1[q] / s2[q]) / scale[q];
+  for (int q = 0; q < 4; ++q) {
+    const float neg = -retOff[q];
+    retOff[q] = neg * srcFac[q] + (float)((double)srcFac[q] * 0.5);
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+FLOF_API const char *flof_version(void) { return "flof-gb300 0.1 (sm_103a)"; }
+FLOF_API const char *flof_last_error(void) { return g_last_error.c_str(); }
+FLOF_API const char *flof_status_string(int s) {
+  switch (s) {
+    case FLOF_OK: return "ok";
+    case FLOF_E_ARG: return "invalid argument";
+    case FLOF_E_CUDA: return "CUDA error";
+    case FLOF_E_OOM: return "out of device memory";
+    case FLOF_E_NAN: return "non-finite value";
+    case FLOF_E_STALL: return "solve stalled";
+    case FLOF_E_TIMEOUT: return "device wait timed out";
+    case FLOF_E_STATE: return "call out of order";
+    case FLOF_E_NOTFOUND: return "not found";
+    default: return "unknown status";
+  }
+}
+
+FLOF_API void flof_of_params_default(flof_of_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->wSmooth = 0.f;
+  p->wEnergy = 0.f;
+  p->level = 0;
+  p->postVelBlur = 0.f;
+  p->cgAccuracy = 1e-04f;
+  p->blurType = 1;
+  p->cfl = 999.f;
+  p->orderTime = 1;
+  p->orderSpace = 1;
+  p->resetBndWidth = -1.f;
+  p->multiStep = 1;
+  p->projSizeThresh = 9999;
+  p->minGridSize = 10;
+  p->doFinalProject = 0;
+  p->cgMaxIter = 1000;
+}
+
+FLOF_API void flof_of_params_flof(flof_of_params *p) {
+  flof_of_params_default(p);
+  if (!p) return;
+  p->wSmooth = 0.001f;
+  p->wEnergy = 0.0001f;
+  p->cgAccuracy = 0.01f;
+  p->postVelBlur = 4.f;
+  p->cfl = 999.f;
+  p->multiStep = 3;
+  p->minGridSize = 20;
+  p->doFinalProject = 1;
+  p->resetBndWidth = 0.1f;
+}
+
+FLOF_API int flof_ctx_create(int device, flof_ctx **out) {
+  return guarded([&] {
+    need(out != nullptr, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    need(device >= 0 && device < n, "no such CUDA device");
+    CK(cudaSetDevice(device));
+    flof_ctx *c = new flof_ctx();
+    c->device = device;
+    try {
+      CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+      c->stream = c->own_stream;
+      const int maxBlocks = sm_count() * 16 + 64;
+      CK(cudaMalloc(&c->st, sizeof(CGState)));
+      CK(cudaMemset(c->st, 0, sizeof(CGState)));
+      CK(cudaMallocHost(&c->st_h, sizeof(CGState)));
+      CK(cudaMalloc(&c->dpart, sizeof(double) * maxBlocks));
+      CK(cudaMalloc(&c->fpart, sizeof(float) * maxBlocks));
+      CK(cudaMalloc(&c->counter, sizeof(unsigned int) * 8));
+      CK(cudaMemset(c->counter, 0, sizeof(unsigned int) * 8));
+      CK(cudaMalloc(&c->fres, sizeof(float) * 16));
+      CK(cudaMalloc(&c->dres, sizeof(double) * 16));
+      CK(cudaMallocHost(&c->fres_h, sizeof(float) * 16));
+      CK(cudaMallocHost(&c->dres_h, sizeof(double) * 16));
+      CK(cudaDeviceSynchronize());
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+FLOF_API int flof_ctx_destroy(flof_ctx *c) {
+  if (!c) return FLOF_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->lats)
+    if (kv.second.vt) c->pool.put(kv.second.vt);
+  c->lats.clear();
+  c->pool.release_all();
+  cudaFree(c->st);
+  cudaFreeHost(c->st_h);
+  cudaFree(c->dpart);
+  cudaFree(c->fpart);
+  cudaFree(c->counter);
+  cudaFree(c->fres);
+  cudaFree(c->dres);
+  cudaFreeHost(c->fres_h);
+  cudaFreeHost(c->dres_h);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return FLOF_OK;
+}
+
+FLOF_API int flof_ctx_synchronize(flof_ctx *c) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+FLOF_API int flof_ctx_set_stream(flof_ctx *c, void *stream) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  });
+}
+
+FLOF_API void *flof_ctx_stream(flof_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+FLOF_API long long flof_ctx_kernel_launches(flof_ctx *c) { return c ? c->launches : 0; }
+
+FLOF_API int flof_ctx_profile(flof_ctx *c, int enable) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    c->recs.clear();
+    c->ev_used = 0;
+    c->profiling = enable ? 1 : 0;
+  });
+}
+
+FLOF_API int flof_ctx_profile_count(flof_ctx *c, int *n) {
+  return guarded([&] {
+    need(c != nullptr && n != nullptr, "NULL argument");
+    CK(cudaStreamSynchronize(c->stream));
+    *n = (int)c->recs.size();
+  });
+}
+
+FLOF_API int flof_ctx_profile_record(flof_ctx *c, int i, int *cls, int *size_x, double *bytes,
+                                     float *ms) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need(i >= 0 && i < (int)c->recs.size(), "record index out of range");
+    const ProfRec &r = c->recs[i];
+    if (cls) *cls = r.cls;
+    if (size_x) *size_x = r.size_x;
+    if (bytes) *bytes = r.bytes;
+    if (ms) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, r.e0, r.e1));
+      *ms = t;
+    }
+  });
+}
+
+FLOF_API const char *flof_kernel_class_name(int cls) {
+  if (cls < 0 || cls >= KC_COUNT) return "unknown";
+  return kc_names[cls];
+}
+
+FLOF_API int flof_ctx_trim(flof_ctx *c) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    c->pool.trim();
+  });
+}
+
+// ---- grids -------------------------------------------------------------------
+
+FLOF_API int flof_grid_create(flof_ctx *c, const int dims[4], int elem, flof_grid **out) {
+  return guarded([&] {
+    need(c != nullptr && dims != nullptr && out != nullptr, "NULL argument");
+    need(elem == FLOF_REAL || elem == FLOF_VEC4, "elem must be FLOF_REAL or FLOF_VEC4");
+    for (int q = 0; q < 4; ++q) need(dims[q] >= 1, "grid extents must be positive");
+    const long long cells = (long long)dims[0] * dims[1] * dims[2] * dims[3];
+    need(cells < (1ll << 31), "grid too large (cells must stay below 2^31)");
+    set_ctx_device(c);
+    flof_grid *g = new flof_grid();
+    g->ctx = c;
+    memcpy(g->dims, dims, sizeof(g->dims));
+    g->elem = elem;
+    size_t bytes = g->bytes();
+    cudaError_t e = cudaMalloc(&g->d, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      delete g;
+      fail(FLOF_E_OOM, "device allocation of a grid failed");
+    }
+    g->owned = true;
+    cudaError_t e2 = cudaMemsetAsync(g->d, 0, bytes, c->stream);
+    if (e2 != cudaSuccess) {
+      cudaFree(g->d);
+      delete g;
+      cuda_check(e2, "cudaMemsetAsync");
+    }
+    *out = g;
+  });
+}
+
+FLOF_API int flof_grid_wrap(flof_ctx *c, const int dims[4], int elem, void *ptr,
+                            flof_grid **out) {
+  return guarded([&] {
+    need(c != nullptr && dims != nullptr && out != nullptr, "NULL argument");
+    need(elem == FLOF_REAL || elem == FLOF_VEC4, "elem must be FLOF_REAL or FLOF_VEC4");
+    for (int q = 0; q < 4; ++q) need(dims[q] >= 1, "grid extents must be positive");
+    need(ptr != nullptr, "device pointer is NULL");
+    need(((uintptr_t)ptr & 15) == 0, "device pointer must be 16-byte aligned");
+    const long long cells = (long long)dims[0] * dims[1] * dims[2] * dims[3];
+    need(cells < (1ll << 31), "grid too large (cells must stay below 2^31)");
+    flof_grid *g = new flof_grid();
+    g->ctx = c;
+    memcpy(g->dims, dims, sizeof(g->dims));
+    g->elem = elem;
+    g->d = ptr;
+    g->owned = false;
+    *out = g;
+  });
+}
+
+FLOF_API int flof_grid_destroy(flof_grid *g) {
+  if (!g) return FLOF_OK;
+  if (g->owned && g->d) {
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    cudaFree(g->d);
+  }
+  delete g;
+  return FLOF_OK;
+}
+
+FLOF_API int flof_grid_dims(const flof_grid *g, int dims[4], int *elem) {
+  return guarded([&] {
+    need(g != nullptr, "grid is NULL");
+    if (dims) memcpy(dims, g->dims, sizeof(g->dims));
+    if (elem) *elem = g->elem;
+  });
+}
+
+FLOF_API void *flof_grid_data(flof_grid *g) { return g ? g->d : nullptr; }
+
+FLOF_API int flof_grid_upload(flof_grid *g, const void *host) {
+  return guarded([&] {
+    need_grid(g, "grid");
+    need(host != nullptr, "host buffer is NULL");
+    set_ctx_device(g->ctx);
+    CK(cudaMemcpyAsync(g->d, host, g->bytes(), cudaMemcpyHostToDevice, g->ctx->stream));
+    CK(cudaStreamSynchronize(g->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_download(const flof_grid *g, void *host) {
+  return guarded([&] {
+    need_grid(g, "grid");
+    need(host != nullptr, "host buffer is NULL");
+    set_ctx_device(g->ctx);
+    CK(cudaMemcpyAsync(host, g->d, g->bytes(), cudaMemcpyDeviceToHost, g->ctx->stream));
+    CK(cudaStreamSynchronize(g->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_copyFrom(flof_grid *dst, const flof_grid *src) {
+  return guarded([&] {
+    need_grid(dst, "dst");
+    need_grid(src, "src");
+    same_size(dst, src, "copyFrom");
+    need(dst->elem == src->elem, "copyFrom: element types differ");
+    CK(cudaMemcpyAsync(dst->d, src->d, dst->bytes(), cudaMemcpyDeviceToDevice,
+                       dst->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_add(flof_grid *a, const flof_grid *b) {
+  return guarded([&] {
+    need_grid(a, "a");
+    need_grid(b, "b");
+    same_size(a, b, "add");
+    need(a->elem == b->elem, "add: element types differ");
+    KL(a->ctx, launch_add(a->f(), b->f(), a->cells() * a->nc(), a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_sub(flof_grid *a, const flof_grid *b) {
+  return guarded([&] {
+    need_grid(a, "a");
+    need_grid(b, "b");
+    same_size(a, b, "sub");
+    need(a->elem == b->elem, "sub: element types differ");
+    KL(a->ctx, launch_sub(a->f(), b->f(), a->cells() * a->nc(), a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_setConst(flof_grid *a, const float v[4]) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    need(v != nullptr, "value is NULL");
+    KL(a->ctx, launch_set_const(a->f(), a->cells(), a->nc(), f4(v, a->nc()), a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_addConst(flof_grid *a, const float v[4]) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    need(v != nullptr, "value is NULL");
+    KL(a->ctx, launch_add_const(a->f(), a->cells(), a->nc(), f4(v, a->nc()), a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_multConst(flof_grid *a, const float v[4]) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    need(v != nullptr, "value is NULL");
+    KL(a->ctx, launch_mult_const(a->f(), a->cells(), a->nc(), f4(v, a->nc()), a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_addScaled(flof_grid *a, const flof_grid *b, const float factor[4]) {
+  return guarded([&] {
+    need_grid(a, "a");
+    need_grid(b, "b");
+    same_size(a, b, "addScaled");
+    need(a->elem == b->elem, "addScaled: element types differ");
+    need(factor != nullptr, "factor is NULL");
+    KL(a->ctx, launch_add_scaled(a->f(), b->f(), a->cells(), a->nc(), f4(factor, a->nc()),
+                                 a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_clear(flof_grid *a) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    CK(cudaMemsetAsync(a->d, 0, a->bytes(), a->ctx->stream));
+  });
+}
+
+static int grid_reduce(flof_grid *a, int which, float *out) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    need(out != nullptr, "out is NULL");
+    flof_ctx *c = a->ctx;
+    if (a->nc() == 4) {
+      KL(c, launch_reduce_minmax(a->f(), a->cells(), 4, which == 1 ? 1 : 0, c->fpart,
+                                 c->counter + 6, c->fres + 2, c->stream));
+      *out = sqrtf(read_f(c, c->fres + 2));
+      return;
+    }
+    if (which == 2) {
+      KL(c, launch_reduce_minmax(a->f(), a->cells(), 1, 1, c->fpart, c->counter + 6,
+                                 c->fres + 2, c->stream));
+      const float amin = read_f(c, c->fres + 2);
+      KL(c, launch_reduce_minmax(a->f(), a->cells(), 1, 0, c->fpart, c->counter + 6,
+                                 c->fres + 3, c->stream));
+      const float amax = read_f(c, c->fres + 3);
+      const float x = fabsf(amin), y = fabsf(amax);
+      *out = x > y ? x : y;
+      return;
+    }
+    KL(c, launch_reduce_minmax(a->f(), a->cells(), 1, which, c->fpart, c->counter + 6,
+                               c->fres + 2, c->stream));
+    *out = read_f(c, c->fres + 2);
+  });
+}
+
+FLOF_API int flof_grid_getMax(flof_grid *a, float *out) { return grid_reduce(a, 0, out); }
+FLOF_API int flof_grid_getMin(flof_grid *a, float *out) { return grid_reduce(a, 1, out); }
+FLOF_API int flof_grid_getMaxAbs(flof_grid *a, float *out) { return grid_reduce(a, 2, out); }
+
+FLOF_API int flof_grid_setBound(flof_grid *a, const float v[4], int w) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    need(v != nullptr, "value is NULL");
+    KL(a->ctx, launch_set_bound(a->f(), a->D(), a->nc(), f4(v, a->nc()), w, a->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_setBoundNeumann(flof_grid *a, int w) {
+  return guarded([&] {
+    need_grid(a, "grid");
+    for (int q = 0; q < 4; ++q)
+      need(a->dims[q] > 2 * (w + 1), "setBoundNeumann: boundary wider than the grid");
+    KL(a->ctx, launch_set_bound_neumann(a->f(), a->D(), a->nc(), w, a->ctx->stream));
+  });
+}
+
+// ---- plugins --------------------------------------------------------------------
+
+FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flof_grid *i0,
+                                          const flof_grid *i1, const flof_of_params *params,
+                                          float *err, flof_solve_stats *stats) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(vel, "vel");
+    need_grid(i0, "i0");
+    need_grid(i1, "i1");
+    need_elem(vel, FLOF_VEC4, "vel");
+    need_elem(i0, FLOF_REAL, "i0");
+    need_elem(i1, FLOF_REAL, "i1");
+    same_size(vel, i0, "opticalFlowMultiscale4d");
+    same_size(vel, i1, "opticalFlowMultiscale4d");
+    need_4d(vel, "vel");
+    flof_of_params def;
+    flof_of_params_default(&def);
+    const flof_of_params &pp = params ? *params : def;
+    need(pp.blurType == 1 || pp.blurType == 2, "blurType must be 1 or 2");
+    need(pp.cgMaxIter >= 0, "cgMaxIter must be >= 0");
+    need(pp.cfl > 0.f, "cfl must be positive");
+    set_ctx_device(c);
+    const auto t0 = std::chrono::steady_clock::now();
+    flof_solve_stats local;
+    memset(&local, 0, sizeof(local));
+    c->stats = &local;
+    const int syncs0 = c->syncs;
+    MSArgs m;
+    m.wSmooth = pp.wSmooth;
+    m.wEnergy = pp.wEnergy;
+    m.postVelBlur = pp.postVelBlur;
+    m.cgAccuracy = pp.cgAccuracy;
+    m.cfl = pp.cfl;
+    m.resetBndWidth = pp.resetBndWidth;
+    m.blurType = pp.blurType;
+    m.multiStep = pp.multiStep;
+    m.projSizeThresh = pp.projSizeThresh;
+    m.minGridSize = pp.minGridSize;
+    m.doFinalProject = pp.doFinalProject;
+    m.cgMaxIter = pp.cgMaxIter;
+    float e;
+    try {
+      e = multiscale(c, vel->D(), vel->v(), i0->f(), i1->f(), m, pp.level);
+      CK(cudaStreamSynchronize(c->stream));
+    } catch (...) {
+      c->stats = nullptr;
+      throw;
+    }
+    c->stats = nullptr;
+    local.err_final = e;
+    local.syncs = c->syncs - syncs0;
+    local.seconds =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (err) *err = e;
+    if (stats) *stats = local;
+  });
+}
+
+FLOF_API int flof_opticalFlow4d(flof_ctx *c, flof_grid *vel, const flof_grid *i0,
+                                const flof_grid *i1, float wSmooth, float wEnergy,
+                                float postVelBlur, float cgAccuracy, int blurType,
+                                float resetBndWidth, int cgMaxIter, int *iterations,
+                                float *residual) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(vel, "vel");
+    need_grid(i0, "i0");
+    need_grid(i1, "i1");
+    need_elem(vel, FLOF_VEC4, "vel");
+    need_elem(i0, FLOF_REAL, "i0");
+    need_elem(i1, FLOF_REAL, "i1");
+    same_size(vel, i0, "opticalFlow4d");
+    same_size(vel, i1, "opticalFlow4d");
+    need_4d(vel, "vel");
+    need(blurType == 1 || blurType == 2, "blurType must be 1 or 2");
+    set_ctx_device(c);
+    OFArgs a;
+    a.wSmooth = wSmooth;
+    a.wEnergy = wEnergy;
+    a.postVelBlur = postVelBlur;
+    a.cgAccuracy = cgAccuracy;
+    a.resetBndWidth = resetBndWidth;
+    a.blurType = blurType;
+    a.cgMaxIter = cgMaxIter;
+    // the input vel enters the rhs; the result replaces it
+    DBuf vin(c, vel->bytes());
+    CK(cudaMemcpyAsync(vin.p, vel->d, vel->bytes(), cudaMemcpyDeviceToDevice, c->stream));
+    optical_flow_dim(c, vel->D(), vel->v(), vin.v(), i0->f(), i1->f(), a, iterations, residual);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+FLOF_API int flof_corrVelsOf4d(flof_ctx *c, flof_grid *dst, flof_grid *vel,
+                               const flof_grid *phiOrg, const flof_grid *phiCurr,
+                               const flof_grid *phiTarget, float threshPhi, float threshNorm,
+                               float postVelBlur, float resetBndWidth, int maxIter) {
+  (void)phiCurr;
+  (void)threshNorm;
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(dst, "dst");
+    need_grid(vel, "vel");
+    need_grid(phiOrg, "phiOrg");
+    need_grid(phiTarget, "phiTarget");
+    need_elem(dst, FLOF_VEC4, "dst");
+    need_elem(vel, FLOF_VEC4, "vel");
+    need_elem(phiOrg, FLOF_REAL, "phiOrg");
+    need_elem(phiTarget, FLOF_REAL, "phiTarget");
+    same_size(dst, vel, "corrVelsOf4d");
+    same_size(vel, phiOrg, "corrVelsOf4d");
+    same_size(vel, phiTarget, "corrVelsOf4d");
+    need_4d(vel, "vel");
+    set_ctx_device(c);
+    corr_vels_of(c, vel->D(), dst->v(), vel->v(), phiOrg->f(), phiTarget->f(), threshPhi,
+                 postVelBlur, resetBndWidth, maxIter, 1);
+    CK(cudaStreamSynchronize(c->stream));
+  });
+}
+
+FLOF_API int flof_gaussianBlur4d(flof_ctx *c, flof_grid *a, float sigma, int blurType) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(a, "grid");
+    need_4d(a, "grid");
+    need(blurType == 1 || blurType == 2, "blurType must be 1 or 2");
+    set_ctx_device(c);
+    gauss_blur(c, a->f(), a->D(), a->nc(), sigma, blurType);
+  });
+}
+
+FLOF_API int flof_advect4d(flof_ctx *c, const flof_grid *vel, flof_grid *grid, float dtFac) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(vel, "vel");
+    need_grid(grid, "grid");
+    need_elem(vel, FLOF_VEC4, "vel");
+    same_size(vel, grid, "advect4d");
+    need_4d(vel, "vel");
+    set_ctx_device(c);
+    const float dt = 1.0f * dtFac;
+    DBuf fwd(c, grid->bytes());
+    KLP(c, KC_ADVECT, grid->dims[0], grid->cells() * (16 + 8 * grid->nc()),
+        launch_advect(vel->v(), grid->f(), fwd.f(), grid->D(), grid->nc(), dt, c->stream));
+    CK(cudaMemcpyAsync(grid->d, fwd.p, grid->bytes(), cudaMemcpyDeviceToDevice, c->stream));
+  });
+}
+
+FLOF_API int flof_calcLsDiff4d(flof_ctx *c, const flof_grid *i0, const flof_grid *i1,
+                               flof_grid *out, float correction, int bnd, float *result) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(i0, "i0");
+    need_grid(i1, "i1");
+    need_elem(i0, FLOF_REAL, "i0");
+    need_elem(i1, FLOF_REAL, "i1");
+    same_size(i0, i1, "calcLsDiff4d");
+    if (out) {
+      need_elem(out, FLOF_REAL, "out");
+      same_size(i0, out, "calcLsDiff4d");
+    }
+    need(bnd >= 0 && 2 * bnd < i0->dims[0] && 2 * bnd < i0->dims[1] && 2 * bnd < i0->dims[2] &&
+             2 * bnd < i0->dims[3],
+         "calcLsDiff4d: bnd leaves no cells");
+    set_ctx_device(c);
+    const float r = ls_diff(c, i0->f(), i1->f(), out ? out->f() : nullptr, i0->D(), correction,
+                            bnd);
+    if (result) *result = r;
+  });
+}
+
+static int interpolate_common(flof_ctx *c, flof_grid *target, const flof_grid *source,
+                              const float *offset, const float *scale, const float *size,
+                              int elem) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(target, "target");
+    need_grid(source, "source");
+    need_elem(target, elem, "target");
+    need_elem(source, elem, "source");
+    need_4d(source, "source");
+    set_ctx_device(c);
+    const float zero[4] = {0, 0, 0, 0}, one[4] = {1, 1, 1, 1}, neg[4] = {-1, -1, -1, -1};
+    const float *o = offset ? offset : zero, *s = scale ? scale : one, *z = size ? size : neg;
+    float s1[4], s2[4], fac[4], off[4];
+    for (int q = 0; q < 4; ++q) {
+      s1[q] = (float)source->dims[q];
+      s2[q] = (float)target->dims[q];
+      off[q] = o[q];
+    }
+    grid_factor4d(s1, s2, z, s, fac, off);
+    KL(c, launch_resample(target->f(), target->D(), source->f(), source->D(), target->nc(),
+                          make_float4(fac[0], fac[1], fac[2], fac[3]),
+                          make_float4(off[0], off[1], off[2], off[3]), c->stream));
+  });
+}
+
+FLOF_API int flof_interpolateGrid4d(flof_ctx *c, flof_grid *target, const flof_grid *source,
+                                    const float offset[4], const float scale[4],
+                                    const float size[4]) {
+  return interpolate_common(c, target, source, offset, scale, size, FLOF_REAL);
+}
+
+FLOF_API int flof_interpolateGrid4dVec(flof_ctx *c, flof_grid *target, const flof_grid *source,
+                                       const float offset[4], const float scale[4],
+                                       const float size[4]) {
+  return interpolate_common(c, target, source, offset, scale, size, FLOF_VEC4);
+}
+
+FLOF_API int flof_deform4d(flof_ctx *c, flof_grid *out, const flof_grid *i0,
+                           const flof_grid *i1, const flof_grid *vel, const flof_grid *velInv,
+                           float alpha, float alphaInv, int twoway) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(out, "out");
+    need_grid(i0, "i0");
+    need_grid(vel, "vel");
+    need_elem(out, FLOF_REAL, "out");
+    need_elem(i0, FLOF_REAL, "i0");
+    need_elem(vel, FLOF_VEC4, "vel");
+    same_size(out, i0, "deform4d");
+    same_size(out, vel, "deform4d");
+    need_4d(out, "out");
+    need(twoway >= 0 && twoway <= 2, "twoway must be 0, 1 or 2");
+    set_ctx_device(c);
+    const Dims4 d = out->D();
+    if (twoway == 1) {
+      need_grid(i1, "i1");
+      need_grid(velInv, "velInv");
+      need_elem(i1, FLOF_REAL, "i1");
+      need_elem(velInv, FLOF_VEC4, "velInv");
+      same_size(out, i1, "deform4d");
+      same_size(out, velInv, "deform4d");
+      need(out->d != i0->d && out->d != i1->d, "deform4d: out must not alias the inputs");
+      KLP(c, KC_DEFORM, d.x, d.cells() * 44,
+          launch_deform_twoway(vel->v(), velInv->v(), i0->f(), i1->f(), out->f(), d, alpha,
+                                 alphaInv, c->stream));
+      return;
+    }
+    need(out->d != i0->d, "deform4d: out must not alias i0");
+    KLP(c, KC_ADVECT, d.x, d.cells() * 24,
+        launch_advect(vel->v(), i0->f(), out->f(), d, 1, 1.0f * alpha, c->stream));
+    if (twoway == 2) {
+      need_grid(i1, "i1");
+      same_size(out, i1, "deform4d");
+      KL(c, launch_mult_const(out->f(), d.cells(), 1, make_float4(alphaInv, 0, 0, 0), c->stream));
+      KL(c, launch_add_scaled(out->f(), i1->f(), d.cells(), 1, make_float4(alpha, 0, 0, 0),
+                              c->stream));
+    }
+  });
+}
+
+// ---- mode-3 slice application ---------------------------------------------------------
+
+FLOF_API int flof_loadAdvectTimeSlice_OptInit(flof_ctx *c, int id, const flof_grid *defo,
+                                              int useDefoVols, int doAligned,
+                                              float partialLoadFac) {
+  (void)doAligned;
+  (void)partialLoadFac;
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(defo, "defo");
+    need_elem(defo, FLOF_VEC4, "defo");
+    need(!useDefoVols, "deformation volumes (useDefoVols) are not supported");
+    // the trilinear slice sample reads a 2x2x2 neighbourhood
+    need(defo->dims[0] >= 2 && defo->dims[1] >= 2 && defo->dims[2] >= 2 && defo->dims[3] >= 1,
+         "Invalid src size of the deformation (x, y, z extents must be at least 2)");
+    set_ctx_device(c);
+    LatsData &L = c->lats[id];
+    if (L.vt) c->pool.put(L.vt);
+    L.defo = defo;
+    L.vt = c->pool.get((size_t)defo->dims[0] * defo->dims[1] * defo->dims[2] * sizeof(float4));
+    L.lastT = -1;
+  });
+}
+
+FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *c, int id) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    auto it = c->lats.find(id);
+    if (it == c->lats.end()) return;
+    CK(cudaStreamSynchronize(c->stream));
+    if (it->second.vt) c->pool.put(it->second.vt);
+    c->lats.erase(it);
+  });
+}
+
+namespace {
+
+struct SliceSetup {
+  float sf[4], off2[4];
+  int t, tp1;
+  float tw;
+};
+
+// The size/offset arithmetic of loadAdvectTimeSlice_OptRun
+// (optflow4d.cpp:1961-1985).
+SliceSetup slice_setup(const flof_grid *defo, const flof_grid *phi, float time,
+                       float loadTimeScale, const float *defoOffset, const float *defoScale,
+                       const float *overrideSize) {
+  SliceSetup S;
+  const float dim4[4] = {(float)defo->dims[0], (float)defo->dims[1], (float)defo->dims[2],
+                         (float)defo->dims[3]};
+  int ds[4] = {phi->dims[0], phi->dims[1], phi->dims[2], phi->dims[3]};
+  if (overrideSize && overrideSize[0] > 0.f)
+    for (int q = 0; q < 4; ++q) ds[q] = trunc_f(overrideSize[q]);
+  float defoSize[4], neg1[4] = {-1, -1, -1, -1}, one[4] = {1, 1, 1, 1};
+  for (int q = 0; q < 4; ++q) {
+    defoSize[q] = (float)ds[q];
+    S.off2[q] = defoOffset ? defoOffset[q] : 0.f;
+  }
+  grid_factor4d(dim4, defoSize, neg1, defoScale ? defoScale : one, S.sf, S.off2);
+  const float srcTime = (float)((double)(time * S.sf[3] * loadTimeScale + S.off2[3]) - 0.5);
+  int t = trunc_f(srcTime);
+  int tp1 = t + 1;
+  S.tw = srcTime - (float)t;
+  const int dimT = defo->dims[3];
+  if (t > dimT - 1) t = dimT - 1;
+  if (tp1 > dimT - 1) tp1 = dimT - 1;
+  need(t >= 0 && tp1 >= 0, "loadAdvectTimeSlice: time maps before the first deformation slice");
+  S.t = t;
+  S.tp1 = tp1;
+  return S;
+}
+
+void blend_vt(flof_ctx *c, LatsData &L, const SliceSetup &S, int zeroVel) {
+  const flof_grid *defo = L.defo;
+  const long long slice = (long long)defo->dims[0] * defo->dims[1] * defo->dims[2];
+  const float4 *base = defo->v();
+  if (zeroVel) {
+    CK(cudaMemsetAsync(L.vt, 0, slice * sizeof(float4), c->stream));
+  } else {
+    KLP(c, KC_BLEND, defo->dims[0], slice * 48,
+        launch_blend_slices(base + (long long)S.t * slice, base + (long long)S.tp1 * slice,
+                              (float4 *)L.vt, slice, 1.0f - S.tw, S.tw, c->stream));
+  }
+  L.lastT = S.t;
+}
+
+LatsData &lats_of(flof_ctx *c, int id) {
+  auto it = c->lats.find(id);
+  if (it == c->lats.end() || !it->second.defo)
+    fail(FLOF_E_STATE, "Load-advect data id " + std::to_string(id) + " not initialized!");
+  return it->second;
+}
+
+}  // namespace
+
+FLOF_API int flof_loadAdvectTimeSlice_OptRun(
+    flof_ctx *c, int id, flof_grid *dst, const flof_grid *phi, float time, float blendAlpha,
+    float loadTimeScale, const float defoOffset[4], const float defoScale[4],
+    const float defoFactor[4], const float overrideSize[4], float overrideTimeOff, int zeroVel,
+    float thirdAlpha, int bordSkip, float fourthAlpha, float defoAniFac) {
+  (void)thirdAlpha;
+  (void)fourthAlpha;
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(dst, "dst");
+    need_grid(phi, "phi");
+    need_elem(dst, FLOF_REAL, "dst");
+    need_elem(phi, FLOF_REAL, "phi");
+    need(dst->dims[3] == 1, "dst must be a 3D grid (t extent 1)");
+    need_4d(phi, "phi");
+    set_ctx_device(c);
+    LatsData &L = lats_of(c, id);
+    const SliceSetup S =
+        slice_setup(L.defo, phi, time, loadTimeScale, defoOffset, defoScale, overrideSize);
+    blend_vt(c, L, S, zeroVel);
+    const float one[4] = {1, 1, 1, 1};
+    const float *dfac = defoFactor ? defoFactor : one;
+    const float4 df = make_float4(dfac[0] * defoAniFac, dfac[1] * defoAniFac,
+                                  dfac[2] * defoAniFac, dfac[3] * defoAniFac);
+    KLP(c, KC_LOOKUP, dst->dims[0], dst->cells() * 8,
+        launch_lookup_slice(dst->f(), dst->dims[0], dst->dims[1], dst->dims[2], phi->f(),
+                              phi->D(), time + overrideTimeOff, blendAlpha,
+                              (const float4 *)L.vt, L.defo->dims[0], L.defo->dims[1],
+                              L.defo->dims[2], make_float4(S.sf[0], S.sf[1], S.sf[2], 0.f),
+                              make_float4(S.off2[0], S.off2[1], S.off2[2], 0.f), df, bordSkip,
+                              c->stream));
+  });
+}
+
+FLOF_API int flof_loadAdvectTimeSlice_OptRunTwoway(
+    flof_ctx *c, int id0, int id1, flof_grid *dst, const flof_grid *phi0,
+    const flof_grid *phi1, float time, float blendAlpha, float alphaInv, float loadTimeScale,
+    const float defoOffset[4], const float defoScale[4], const float defoFactor[4],
+    const float overrideSize[4], float overrideTimeOff, int bordSkip, float defoAniFac) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need_grid(dst, "dst");
+    need_grid(phi0, "phi0");
+    need_grid(phi1, "phi1");
+    need_elem(dst, FLOF_REAL, "dst");
+    need(dst->dims[3] == 1, "dst must be a 3D grid (t extent 1)");
+    same_size(phi0, phi1, "OptRunTwoway");
+    need_4d(phi0, "phi0");
+    set_ctx_device(c);
+    LatsData &L0 = lats_of(c, id0);
+    LatsData &L1 = lats_of(c, id1);
+    need(L0.defo->dims[0] == L1.defo->dims[0] && L0.defo->dims[1] == L1.defo->dims[1] &&
+             L0.defo->dims[2] == L1.defo->dims[2] && L0.defo->dims[3] == L1.defo->dims[3],
+         "OptRunTwoway: both deformations must have the same size");
+    const SliceSetup S0 =
+        slice_setup(L0.defo, phi0, time, loadTimeScale, defoOffset, defoScale, overrideSize);
+    const SliceSetup S1 =
+        slice_setup(L1.defo, phi1, time, loadTimeScale, defoOffset, defoScale, overrideSize);
+    blend_vt(c, L0, S0, 0);
+    blend_vt(c, L1, S1, 0);
+    const float one[4] = {1, 1, 1, 1};
+    const float *dfac = defoFactor ? defoFactor : one;
+    const float4 df = make_float4(dfac[0] * defoAniFac, dfac[1] * defoAniFac,
+                                  dfac[2] * defoAniFac, dfac[3] * defoAniFac);
+    KLP(c, KC_LOOKUP, dst->dims[0], dst->cells() * 12,
+        launch_lookup_slice_twoway(
+              dst->f(), dst->dims[0], dst->dims[1], dst->dims[2], phi0->f(), phi1->f(),
+              phi0->D(), time + overrideTimeOff, blendAlpha, alphaInv, (const float4 *)L0.vt,
+              (const float4 *)L1.vt, L0.defo->dims[0], L0.defo->dims[1], L0.defo->dims[2],
+              make_float4(S0.sf[0], S0.sf[1], S0.sf[2], 0.f),
+              make_float4(S0.off2[0], S0.off2[1], S0.off2[2], 0.f), df, bordSkip, c->stream));
+  });
+}
+
+}  // extern "C"

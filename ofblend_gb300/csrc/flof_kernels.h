@@ -1,0 +1,148 @@
+// flof_kernels.h -- host-side launchers of the FlOF CUDA kernels.  Every
+// launcher enqueues work on the given stream and returns immediately; errors
+// surface through cudaGetLastError() / the next synchronisation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "flof_common.cuh"
+
+namespace flof {
+
+// Number of SMs of the current device (cached), used to size grids.
+int sm_count();
+// Blocks for a grid-stride launch over n items with `nt` threads per block.
+int grid_for(long long n, int nt, int per_sm = 8);
+
+// ---- elementwise (n = number of floats) -----------------------------------
+void launch_set_const(float *a, long long ncell, int nc, float4 v, cudaStream_t s);
+void launch_add_const(float *a, long long ncell, int nc, float4 v, cudaStream_t s);
+void launch_mult_const(float *a, long long ncell, int nc, float4 v, cudaStream_t s);
+void launch_add(float *a, const float *b, long long n, cudaStream_t s);
+void launch_sub(float *a, const float *b, long long n, cudaStream_t s);
+// a += factor * b, per component
+void launch_add_scaled(float *a, const float *b, long long ncell, int nc, float4 f,
+                       cudaStream_t s);
+
+// ---- borders -----------------------------------------------------------------
+void launch_set_bound(float *a, Dims4 d, int nc, float4 v, int w, cudaStream_t s);
+void launch_set_bound_neumann(float *a, Dims4 d, int nc, int w, cudaStream_t s);
+// zero every cell outside isInBounds(resetBnd)
+void launch_reset_outside(float4 *a, Dims4 d, int resetBnd, cudaStream_t s);
+
+// ---- reductions (result written to device memory) ---------------------------
+// which: 0 max, 1 min.  For nc == 4 the value is max/min |v|^2 (no sqrt).
+// `partials` holds grid_for(...) floats, `counter` one zeroed uint.
+void launch_reduce_minmax(const float *a, long long ncell, int nc, int which,
+                          float *partials, unsigned int *counter, float *result,
+                          cudaStream_t s);
+// calcLsDiffTempl sum over the bnd box (double), scaled as the reference
+// does; result as double and as float.
+void launch_ls_diff(const float *i0, const float *i1, float *out, Dims4 d,
+                    float correction, int bnd, double *partials,
+                    unsigned int *counter, double *result_d, float *result_f,
+                    cudaStream_t s);
+int ls_diff_blocks(Dims4 d, int bnd);
+
+// ---- resampling / advection ---------------------------------------------------
+void launch_resample(float *target, Dims4 td, const float *source, Dims4 sd,
+                     int nc, float4 fac, float4 off, cudaStream_t s);
+// dst (fresh) = src sampled at ijkt+0.5 - vel*dt over bnd=1 cells; the
+// border ring of dst is written with zeros.
+void launch_advect(const float4 *vel, const float *src, float *dst, Dims4 d,
+                   int nc, float dt, cudaStream_t s);
+// Two-way blend of deform4d (scenes/flof.py:603-610) in one pass:
+// out = (advect(vel,i0,a) * (1-a)) + a * advect(velInv,i1,1-a).
+void launch_deform_twoway(const float4 *vel, const float4 *velInv,
+                          const float *i0, const float *i1, float *out, Dims4 d,
+                          float alpha, float alphaInv, cudaStream_t s);
+
+// ---- mode-3 slice lookup -------------------------------------------------------
+// vt = (0 + f1*v1) + f2*v2 over one defo t-slice of `cells` cells
+void launch_blend_slices(const float4 *v1, const float4 *v2, float4 *vt,
+                         long long cells, float f1, float f2, cudaStream_t s);
+void launch_lookup_slice(float *dst, int dx, int dy, int dz, const float *phi,
+                         Dims4 pd, float time, float dt, const float4 *vt,
+                         int vx, int vy, int vz, float4 sf3, float4 off3,
+                         float4 defoFactor, int bordSkip, cudaStream_t s);
+// Both directions of a two-way frame plus the blend of scenes/flof.py
+// :750-755, in one pass.
+void launch_lookup_slice_twoway(float *dst, int dx, int dy, int dz,
+                                const float *phi0, const float *phi1, Dims4 pd,
+                                float time, float alpha, float alphaInv,
+                                const float4 *vt0, const float4 *vt1, int vx,
+                                int vy, int vz, float4 sf3, float4 off3,
+                                float4 defoFactor, int bordSkip, cudaStream_t s);
+
+// ---- optical flow system and PCG ---------------------------------------------------
+struct CGState {
+  double sigma;     // z . r of the current iterate
+  double alpha;     // sigma / (p . A p)
+  double beta;      // sigmaNew / sigma
+  double acc;       // accuracy * max(r0)
+  double resIni;    // max(r0)
+  double pAp;
+  float resMax;     // max(r) after the last update
+  float retResidual;  // resMax / resIni
+  int done;         // 0 running; see CG_* below
+  int iters;
+  unsigned int counter[4];
+};
+enum { CG_RUNNING = 0, CG_CONVERGED = 1, CG_FAILED_SIGMA = 2, CG_EARLY = 3,
+       CG_MAXITER = 4 };
+
+struct OFConsts {
+  float dxf;        // 1 / (2 mDx)
+  float mDx;
+  float mDt;
+  float wSmooth;
+  float wEnergy;
+  float offd;       // -wSmooth * mDx2Inv
+  float diag;       // 8 wSmooth mDx2Inv + wEnergy
+};
+
+int cg_blocks(Dims4 d);
+// Assembly + PCG initialisation over all cells.  vel may be null (zero).
+// Writes g, r = rhs, p = z on the interior, zeros on the border ring, and
+// x = 0 everywhere.
+void launch_of_assemble_init(const float *i0w, const float *i1,
+                             const float4 *vel, float4 *g, float4 *r,
+                             float4 *p, float4 *x, Dims4 d, OFConsts c,
+                             float accuracy, CGState *st, double *dpart,
+                             float *fpart, cudaStream_t s);
+void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s);
+void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
+                      const float4 *g, Dims4 d, OFConsts c, CGState *st,
+                      double *dpart, float *fpart, int iter, int maxIter,
+                      cudaStream_t s);
+void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s);
+// vel = x / mDx over all cells (x border entries are zero)
+void launch_of_copy_back(const float4 *x, float4 *vel, long long cells,
+                         float mDx, const CGState *st, cudaStream_t s);
+
+// ---- Gaussian blur (gaussianBlurGeneric, strict 4D stencil) -----------------
+// One pass of knGaussianBlur over bnd=1 cells; when zero_border, the border
+// ring of dst is written with zeros.  wtab holds exp weights by squared
+// distance (host-computed, as the reference's float(exp(double))).
+void launch_gauss_pass(const float *src, float *dst, Dims4 d, int nc, int s,
+                       const float *wtab, int zero_border, cudaStream_t st);
+// Separable variant (blurType 2): one axis of the 4x1D stencil with
+// in-bounds normalisation; not bitwise equal to the reference.  border_mode
+// 0 writes every cell, 1 interior cells plus a zero ring, 2 interior only.
+void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
+                           int axis, int s, const float *w1d, int border_mode,
+                           cudaStream_t st);
+
+// ---- projection correction ------------------------------------------------------
+void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
+                          const float *phiTarget, float *marker, Dims4 d,
+                          float threshPhi, int maxIter, cudaStream_t s);
+// one knCvExpolBlur4d sweep fused with the copy: out = unmarked interior ?
+// avg81(in) : in
+void launch_expol_sweep(const float4 *in, float4 *out, const float *mark,
+                        Dims4 d, cudaStream_t s);
+
+}  // namespace flof

@@ -1,0 +1,635 @@
+// flof_solve.cu -- optical-flow system assembly, Jacobi-PCG, Gaussian velocity
+// blur and the level-set projection correction.
+//
+// Reference: source/plugin/optflow4d.cpp
+//   opticalFlowDim        :361-553   (assembly :398-493, copy back :520-529)
+//   FixedMatrixOF/applyMat :179-232  (matrix-free here: the block is g g^T +
+//                                     diag I, rebuilt from the stored g)
+//   GridCGOptflow4d        :268-355
+//   knGaussianBlur         :132-158
+//   knProjectCells et al.  :651-734
+//   knCvExpolBlur4d        :613-626
+#include <float.h>
+
+#include "flof_kernels.h"
+
+namespace flof {
+
+constexpr int NT = 256;
+
+// ---------------------------------------------------------------------------
+// Assembly + PCG initialisation
+// ---------------------------------------------------------------------------
+
+int cg_blocks(Dims4 d) {
+  long long n = (long long)(d.x - 2) * (d.y - 2) * (d.z - 2) * (d.t - 2);
+  return grid_for(n > 0 ? n : 1, NT, 8);
+}
+
+static inline BoxDecoder interior_decoder(Dims4 d) {
+  return make_decoder(d.x - 2 > 0 ? d.x - 2 : 1, d.y - 2 > 0 ? d.y - 2 : 1,
+                      d.z - 2 > 0 ? d.z - 2 : 1, 1, 1, 1, 1);
+}
+static inline uint32_t interior_count(Dims4 d) {
+  if (d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3) return 0;
+  return (uint32_t)((long long)(d.x - 2) * (d.y - 2) * (d.z - 2) * (d.t - 2));
+}
+
+// Jacobi preconditioner of row (cell,d): 1/blockd[d][d] with the diagonal
+// g_d*g_d + diag, rounded like the reference's (float)(1./diag).
+__device__ __forceinline__ float4 precond_of(const float4 g, float diag) {
+  float4 p;
+  p.x = __frcp_rn(g.x * g.x + diag);
+  p.y = __frcp_rn(g.y * g.y + diag);
+  p.z = __frcp_rn(g.z * g.z + diag);
+  p.w = __frcp_rn(g.w * g.w + diag);
+  return p;
+}
+
+__global__ void __launch_bounds__(NT)
+k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
+                   const float4 *__restrict__ vel, float4 *__restrict__ g,
+                   float4 *__restrict__ r, float4 *__restrict__ p,
+                   float4 *__restrict__ x, Dims4 d, BoxDecoder bx, uint32_t ncells,
+                   OFConsts c, float accuracy, CGState *st, double *dpart,
+                   float *fpart) {
+  __shared__ double shd[NT / 32];
+  __shared__ float shf[NT / 32];
+  double dot = 0.0;
+  float mx = -FLT_MAX;
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ncells;
+       q += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(q, i, j, k, l);
+    const idx_t id = q;
+    x[id] = zero4;  // setConst(result, 0) (optflow4d.cpp:280)
+    if (!in_bounds(d, i, j, k, l, 1)) {
+      // identity rows with zero rhs (optflow4d.cpp:424-433): g = r = p = 0
+      g[id] = zero4;
+      r[id] = zero4;
+      p[id] = zero4;
+      continue;
+    }
+    const float tderiv = (__ldg(i1 + id) - __ldg(i0w + id)) / c.mDt;
+    float gr[4];
+    gr[0] = (__ldg(i1 + id + 1) - __ldg(i1 + id - 1)) * c.dxf;
+    gr[1] = (__ldg(i1 + id + sY) - __ldg(i1 + id - sY)) * c.dxf;
+    gr[2] = (__ldg(i1 + id + sZ) - __ldg(i1 + id - sZ)) * c.dxf;
+    gr[3] = (__ldg(i1 + id + sT) - __ldg(i1 + id - sT)) * c.dxf;
+    float rh[4];
+#pragma unroll
+    for (int dd = 0; dd < 4; ++dd) rh[dd] = -gr[dd] * tderiv;
+    if (vel) {
+      // rhs -= wSmooth (v - v_nb) mDx mDx2Inv for m = -t,-z,-y,-x,+x,+y,+z,+t,
+      // then -= wEnergy v mDx (optflow4d.cpp:450-478)
+      const float4 vc = __ldg(vel + id);
+      const idx_t off[8] = {-sT, -sZ, -sY, -1, 1, sY, sZ, sT};
+      const float vcc[4] = {vc.x, vc.y, vc.z, vc.w};
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const float4 vn = __ldg(vel + id + off[m]);
+        const float vnn[4] = {vn.x, vn.y, vn.z, vn.w};
+#pragma unroll
+        for (int dd = 0; dd < 4; ++dd)
+          rh[dd] -= c.wSmooth * (vcc[dd] - vnn[dd]) * c.mDx * 1.0f;
+      }
+#pragma unroll
+      for (int dd = 0; dd < 4; ++dd) rh[dd] -= c.wEnergy * vcc[dd] * c.mDx;
+    }
+    const float4 gg = make_float4(gr[0], gr[1], gr[2], gr[3]);
+    const float4 rr = make_float4(rh[0], rh[1], rh[2], rh[3]);
+    const float4 pre = precond_of(gg, c.diag);
+    const float4 z = make_float4(rr.x * pre.x, rr.y * pre.y, rr.z * pre.z, rr.w * pre.w);
+    g[id] = gg;
+    r[id] = rr;
+    p[id] = z;
+    dot += (double)(z.x * rr.x);
+    dot += (double)(z.y * rr.y);
+    dot += (double)(z.z * rr.z);
+    dot += (double)(z.w * rr.w);
+    mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
+  }
+  const double bd = block_sum<NT>(dot, shd);
+  const float bm = block_max<NT>(mx, shf);
+  if (threadIdx.x == 0) {
+    dpart[blockIdx.x] = bd;
+    fpart[blockIdx.x] = bm;
+  }
+  if (last_block_arrives(&st->counter[0])) {
+    double s = 0.0;
+    float m = 0.0f;  // border rows hold r = 0
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += blockDim.x) {
+      s += __ldcg(dpart + q);
+      m = fmaxf(m, __ldcg(fpart + q));
+    }
+    s = block_sum<NT>(s, shd);
+    m = block_max<NT>(m, shf);
+    if (threadIdx.x == 0) {
+      const double residual = (double)m;
+      st->resIni = residual;
+      st->resMax = m;
+      st->iters = 0;
+      st->counter[0] = 0;
+      if (residual < (double)1e-6f) {
+        st->retResidual = 0.f;
+        st->done = CG_EARLY;
+      } else {
+        st->acc = (double)accuracy * residual;
+        st->sigma = s;
+        if (s == 0.0 || s != s) st->done = CG_FAILED_SIGMA;
+        else st->done = CG_RUNNING;
+      }
+    }
+  }
+}
+
+void launch_of_assemble_init(const float *i0w, const float *i1,
+                             const float4 *vel, float4 *g, float4 *r,
+                             float4 *p, float4 *x, Dims4 d, OFConsts c,
+                             float accuracy, CGState *st, double *dpart,
+                             float *fpart, cudaStream_t s) {
+  k_of_assemble_init<<<cg_blocks(d), NT, 0, s>>>(
+      i0w, i1, vel, g, r, p, x, d, make_decoder(d.x, d.y, d.z, 0, 0, 0, 0),
+      (uint32_t)d.cells(), c, accuracy, st, dpart, fpart);
+}
+
+// ---------------------------------------------------------------------------
+// PCG iteration (GridCGOptflow4d::solve, optflow4d.cpp:304-326)
+// ---------------------------------------------------------------------------
+
+// q = A p over the interior rows; applyMat order: 8 neighbour terms
+// (-t,-z,-y,-x,+x,+y,+z,+t) then the 4 block terms.
+__global__ void __launch_bounds__(NT)
+k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
+            float4 *__restrict__ q, Dims4 d, BoxDecoder bx, uint32_t nint,
+            OFConsts c, CGState *st, double *dpart) {
+  if (st->done) return;
+  __shared__ double shd[NT / 32];
+  double dot = 0.0;
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  const float o = c.offd;
+  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
+       n += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    const float4 pc = __ldg(p + id);
+    const float4 gg = __ldg(g + id);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (o != 0.f) {
+      const idx_t off[8] = {-sT, -sZ, -sY, -1, 1, sY, sZ, sT};
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const float4 pn = __ldg(p + id + off[m]);
+        v.x += o * pn.x;
+        v.y += o * pn.y;
+        v.z += o * pn.z;
+        v.w += o * pn.w;
+      }
+    }
+    const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+    const float pv[4] = {pc.x, pc.y, pc.z, pc.w};
+    float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int dd = 0; dd < 4; ++dd) {
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        float b = gv[dd] * gv[m];
+        if (dd == m) b = b + c.diag;
+        vv[dd] += b * pv[m];
+      }
+    }
+    const float4 qq = make_float4(vv[0], vv[1], vv[2], vv[3]);
+    q[id] = qq;
+    dot += (double)(pc.x * qq.x);
+    dot += (double)(pc.y * qq.y);
+    dot += (double)(pc.z * qq.z);
+    dot += (double)(pc.w * qq.w);
+  }
+  const double bd = block_sum<NT>(dot, shd);
+  if (threadIdx.x == 0) dpart[blockIdx.x] = bd;
+  if (last_block_arrives(&st->counter[1])) {
+    double s = 0.0;
+    for (int q2 = threadIdx.x; q2 < (int)gridDim.x; q2 += blockDim.x) s += __ldcg(dpart + q2);
+    s = block_sum<NT>(s, shd);
+    if (threadIdx.x == 0) {
+      st->pAp = s;
+      st->alpha = st->sigma / s;
+      st->counter[1] = 0;
+    }
+  }
+}
+
+void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s) {
+  k_cg_matvec<<<cg_blocks(d), NT, 0, s>>>(p, g, q, d, interior_decoder(d),
+                                          interior_count(d), c, st, dpart);
+}
+
+// x += alpha p; r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).
+__global__ void __launch_bounds__(NT)
+k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
+            const float4 *__restrict__ p, const float4 *__restrict__ q,
+            const float4 *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
+            OFConsts c, CGState *st, double *dpart, float *fpart, int iter,
+            int maxIter) {
+  if (st->done) return;
+  __shared__ double shd[NT / 32];
+  __shared__ float shf[NT / 32];
+  const float a = (float)st->alpha;
+  double dot = 0.0;
+  float mx = -FLT_MAX;
+  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
+       n += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = __ldg(g + id);
+    float4 xx = x[id], rr = r[id];
+    xx.x = __fmaf_rn(a, pp.x, xx.x);
+    xx.y = __fmaf_rn(a, pp.y, xx.y);
+    xx.z = __fmaf_rn(a, pp.z, xx.z);
+    xx.w = __fmaf_rn(a, pp.w, xx.w);
+    rr.x = __fmaf_rn(-a, qq.x, rr.x);
+    rr.y = __fmaf_rn(-a, qq.y, rr.y);
+    rr.z = __fmaf_rn(-a, qq.z, rr.z);
+    rr.w = __fmaf_rn(-a, qq.w, rr.w);
+    x[id] = xx;
+    r[id] = rr;
+    const float4 pre = precond_of(gg, c.diag);
+    dot += (double)((rr.x * pre.x) * rr.x);
+    dot += (double)((rr.y * pre.y) * rr.y);
+    dot += (double)((rr.z * pre.z) * rr.z);
+    dot += (double)((rr.w * pre.w) * rr.w);
+    mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
+  }
+  const double bd = block_sum<NT>(dot, shd);
+  const float bm = block_max<NT>(mx, shf);
+  if (threadIdx.x == 0) {
+    dpart[blockIdx.x] = bd;
+    fpart[blockIdx.x] = bm;
+  }
+  if (last_block_arrives(&st->counter[2])) {
+    double s = 0.0;
+    float m = 0.0f;
+    for (int q2 = threadIdx.x; q2 < (int)gridDim.x; q2 += blockDim.x) {
+      s += __ldcg(dpart + q2);
+      m = fmaxf(m, __ldcg(fpart + q2));
+    }
+    s = block_sum<NT>(s, shd);
+    m = block_max<NT>(m, shf);
+    if (threadIdx.x == 0) {
+      const double residual = (double)m;
+      st->resMax = m;
+      st->retResidual = (float)(residual / st->resIni);
+      st->iters = iter + 1;
+      st->counter[2] = 0;
+      if (residual <= st->acc) {
+        st->done = CG_CONVERGED;
+      } else {
+        st->beta = s / st->sigma;
+        st->sigma = s;
+        if (iter + 1 >= maxIter) st->done = CG_MAXITER;
+      }
+    }
+  }
+}
+
+void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
+                      const float4 *g, Dims4 d, OFConsts c, CGState *st,
+                      double *dpart, float *fpart, int iter, int maxIter,
+                      cudaStream_t s) {
+  k_cg_update<<<cg_blocks(d), NT, 0, s>>>(x, r, p, q, g, d, interior_decoder(d),
+                                          interior_count(d), c, st, dpart, fpart,
+                                          iter, maxIter);
+}
+
+// p = z + beta p
+__global__ void __launch_bounds__(NT)
+k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
+               const float4 *__restrict__ g, Dims4 d, BoxDecoder bx,
+               uint32_t nint, OFConsts c, CGState *st) {
+  if (st->done) return;
+  const float b = (float)st->beta;
+  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
+       n += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    const float4 rr = __ldg(r + id), gg = __ldg(g + id);
+    float4 pp = p[id];
+    const float4 pre = precond_of(gg, c.diag);
+    pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
+    pp.y = __fmaf_rn(b, pp.y, rr.y * pre.y);
+    pp.z = __fmaf_rn(b, pp.z, rr.z * pre.z);
+    pp.w = __fmaf_rn(b, pp.w, rr.w * pre.w);
+    p[id] = pp;
+  }
+}
+
+void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s) {
+  k_cg_direction<<<cg_blocks(d), NT, 0, s>>>(p, r, g, d, interior_decoder(d),
+                                             interior_count(d), c, st);
+}
+
+// vel = x / mDx (optflow4d.cpp:520-529); a NaN residual resets the result to
+// zero first (:508-514).
+__global__ void k_of_copy_back(const float4 *__restrict__ x, float4 *__restrict__ vel,
+                               long long n, float mDx, const CGState *st) {
+  const float res = st->retResidual;
+  const bool reset = (res != res);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    float4 v = reset ? make_float4(0.f, 0.f, 0.f, 0.f) : __ldg(x + q);
+    v.x = v.x / mDx;
+    v.y = v.y / mDx;
+    v.z = v.z / mDx;
+    v.w = v.w / mDx;
+    vel[q] = v;
+  }
+}
+void launch_of_copy_back(const float4 *x, float4 *vel, long long cells,
+                         float mDx, const CGState *st, cudaStream_t s) {
+  k_of_copy_back<<<grid_for(cells, NT), NT, 0, s>>>(x, vel, cells, mDx, st);
+}
+
+// ---------------------------------------------------------------------------
+// Gaussian blur (knGaussianBlur, optflow4d.cpp:132-158)
+// ---------------------------------------------------------------------------
+
+struct WTab {
+  float w[160];  // exp weight by squared tap distance, s <= 6
+};
+
+template <int NC>
+__global__ void __launch_bounds__(NT)
+k_gauss_pass(const float *__restrict__ src, float *__restrict__ dst, Dims4 d,
+             BoxDecoder bx, int s, WTab wt, int zero_border) {
+  const uint32_t n = (uint32_t)d.cells();
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(q, i, j, k, l);
+    if (!in_bounds(d, i, j, k, l, 1)) {
+      if (zero_border) {
+        if (NC == 4) ((float4 *)dst)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else dst[q] = 0.f;
+      }
+      continue;
+    }
+    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+    float weight = 0.f;
+    for (int vt = l - s; vt <= l + s; vt++) {
+      if (vt < 0 || vt >= d.t) continue;
+      for (int zk = k - s; zk <= k + s; zk++) {
+        if (zk < 0 || zk >= d.z) continue;
+        for (int yj = j - s; yj <= j + s; yj++) {
+          if (yj < 0 || yj >= d.y) continue;
+          const int base = (vt - l) * (vt - l) + (zk - k) * (zk - k) + (yj - j) * (yj - j);
+          const idx_t row = d.index(0, yj, zk, vt);
+          for (int xi = i - s; xi <= i + s; xi++) {
+            if (xi < 0 || xi >= d.x) continue;
+            const float w = wt.w[base + (xi - i) * (xi - i)];
+            weight += w;
+            if (NC == 4) {
+              const float4 a = __ldg((const float4 *)src + row + xi);
+              val.x += w * a.x;
+              val.y += w * a.y;
+              val.z += w * a.z;
+              val.w += w * a.w;
+            } else {
+              val.x += w * __ldg(src + row + xi);
+            }
+          }
+        }
+      }
+    }
+    if (weight > 1e-6f) {
+      if (NC == 4)
+        ((float4 *)dst)[q] = make_float4(val.x / weight, val.y / weight, val.z / weight,
+                                         val.w / weight);
+      else
+        dst[q] = val.x / weight;
+    } else {
+      if (NC == 4) ((float4 *)dst)[q] = __ldg((const float4 *)src + q);
+      else dst[q] = __ldg(src + q);
+    }
+  }
+}
+
+void launch_gauss_pass(const float *src, float *dst, Dims4 d, int nc, int s,
+                       const float *wtab, int zero_border, cudaStream_t st) {
+  WTab wt;
+  const int nw = 4 * s * s + 1;
+  for (int q = 0; q < 160; ++q) wt.w[q] = q < nw ? wtab[q] : 0.f;
+  BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
+  const int nb = grid_for(d.cells(), NT, 8);
+  if (nc == 4)
+    k_gauss_pass<4><<<nb, NT, 0, st>>>(src, dst, d, bx, s, wt, zero_border);
+  else
+    k_gauss_pass<1><<<nb, NT, 0, st>>>(src, dst, d, bx, s, wt, zero_border);
+}
+
+// One axis of the separable blur: dst = sum_in_bounds w1d * src / sum w1d.
+// border_mode: 0 every cell, 1 interior cells and a zero ring, 2 interior
+// cells only (the ring keeps its previous values).
+template <int NC>
+__global__ void k_gauss_sep(const float *__restrict__ src, float *__restrict__ dst,
+                            Dims4 d, BoxDecoder bx, int axis, int s, WTab w1,
+                            int border_mode) {
+  const uint32_t n = (uint32_t)d.cells();
+  const int ext[4] = {d.x, d.y, d.z, d.t};
+  const idx_t str[4] = {1, d.x, d.sz(), d.st()};
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += gridDim.x * blockDim.x) {
+    int c[4];
+    bx.decode(q, c[0], c[1], c[2], c[3]);
+    if (border_mode != 0 && !in_bounds(d, c[0], c[1], c[2], c[3], 1)) {
+      if (border_mode == 1) {
+        if (NC == 4) ((float4 *)dst)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        else dst[q] = 0.f;
+      }
+      continue;
+    }
+    const int x0 = c[axis];
+    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+    float weight = 0.f;
+    for (int o = -s; o <= s; ++o) {
+      const int xx = x0 + o;
+      if (xx < 0 || xx >= ext[axis]) continue;
+      const float w = w1.w[o < 0 ? -o : o];
+      weight += w;
+      const idx_t id = (idx_t)q + (idx_t)o * str[axis];
+      if (NC == 4) {
+        const float4 a = __ldg((const float4 *)src + id);
+        val.x += w * a.x;
+        val.y += w * a.y;
+        val.z += w * a.z;
+        val.w += w * a.w;
+      } else {
+        val.x += w * __ldg(src + id);
+      }
+    }
+    const float inv = 1.0f / weight;
+    if (NC == 4)
+      ((float4 *)dst)[q] = make_float4(val.x * inv, val.y * inv, val.z * inv, val.w * inv);
+    else
+      dst[q] = val.x * inv;
+  }
+}
+
+void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
+                           int axis, int s, const float *w1d, int border_mode,
+                           cudaStream_t st) {
+  WTab wt;
+  for (int q = 0; q < 160; ++q) wt.w[q] = q <= s ? w1d[q] : 0.f;
+  BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
+  const int nb = grid_for(d.cells(), NT, 8);
+  if (nc == 4)
+    k_gauss_sep<4><<<nb, NT, 0, st>>>(src, dst, d, bx, axis, s, wt, border_mode);
+  else
+    k_gauss_sep<1><<<nb, NT, 0, st>>>(src, dst, d, bx, axis, s, wt, border_mode);
+}
+
+// ---------------------------------------------------------------------------
+// Projection correction (optflow4d.cpp:651-734)
+// ---------------------------------------------------------------------------
+
+__device__ float4 normal_interp(const float *__restrict__ phi, const Dims4 &d, float p0,
+                                float p1, float p2, float p3) {
+  const float h = 0.5f;
+  float4 n;
+  n.x = interp4_real(phi, d, p0 + h, p1, p2, p3) - interp4_real(phi, d, p0 - h, p1, p2, p3);
+  n.y = interp4_real(phi, d, p0, p1 + h, p2, p3) - interp4_real(phi, d, p0, p1 - h, p2, p3);
+  n.z = interp4_real(phi, d, p0, p1, p2 + h, p3) - interp4_real(phi, d, p0, p1, p2 - h, p3);
+  n.w = interp4_real(phi, d, p0, p1, p2, p3 + h) - interp4_real(phi, d, p0, p1, p2, p3 - h);
+  // normalize (util/vector4d.h:331-345)
+  const float len2 = n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w;
+  const float eps2 = 1e-6f * 1e-6f;
+  if (fabs((double)len2 - 1.) < (double)eps2) {
+    // normalized enough
+  } else if (len2 > eps2) {
+    const float nrm = __fsqrt_rn(len2);
+    const float inv = __frcp_rn(nrm);
+    n.x *= inv;
+    n.y *= inv;
+    n.z *= inv;
+    n.w *= inv;
+  } else {
+    n = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  return n;
+}
+
+__global__ void k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
+                                const float *__restrict__ phiOrg,
+                                const float *__restrict__ phiTarget, float *__restrict__ marker,
+                                Dims4 d, BoxDecoder bx, uint32_t nbox, float threshPhi,
+                                int maxIter) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nbox;
+       q += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(q, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    const float dt = 1.0f;
+    const float4 v = __ldg(vel + id);
+    const float p0 = (float)(i + 0.5f) - v.x * dt;
+    const float p1 = (float)(j + 0.5f) - v.y * dt;
+    const float p2 = (float)(k + 0.5f) - v.z * dt;
+    const float p3 = (float)(l + 0.5f) - v.w * dt;
+    const float4 nrm = normal_interp(phiOrg, d, p0, p1, p2, p3);
+    // projectCell (optflow4d.cpp:675-710)
+    float step = 0.25f;
+    if (maxIter < 50) step = 0.5f;
+    int lastDir = 0;
+    const float targetVal = __ldg(phiTarget + id);
+    float vn = interp4_real(phiOrg, d, p0, p1, p2, p3);
+    float dd = (vn - targetVal);
+    for (int s = 0; s < maxIter; ++s) {
+      const float n0 = p0 + (nrm.x * dd) * dt;
+      const float n1 = p1 + (nrm.y * dd) * dt;
+      const float n2 = p2 + (nrm.z * dd) * dt;
+      const float n3 = p3 + (nrm.w * dd) * dt;
+      if (!in_bounds(d, trunc_i(n0), trunc_i(n1), trunc_i(n2), trunc_i(n3), 0)) {
+        s = maxIter;
+        dd = 9999.f;
+        continue;
+      }
+      vn = interp4_real(phiOrg, d, n0, n1, n2, n3);
+      if (vn < targetVal) {
+        if (lastDir < 0) step *= 0.5f;
+        dd += step;
+        lastDir = 1;
+      } else {
+        if (lastDir > 0) step *= 0.5f;
+        dd -= step;
+        lastDir = -1;
+      }
+      if ((double)step < 1e-01) s = maxIter + 1;
+    }
+    if (fabsf(dd) > threshPhi) {
+      dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+      continue;
+    }
+    dst[id] = make_float4(nrm.x * dd, nrm.y * dd, nrm.z * dd, nrm.w * dd);
+    marker[id] = 1.f;
+  }
+}
+
+void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
+                          const float *phiTarget, float *marker, Dims4 d,
+                          float threshPhi, int maxIter, cudaStream_t s) {
+  if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return;
+  BoxDecoder bx = make_decoder(d.x - 4, d.y - 4, d.z - 4, 2, 2, 2, 2);
+  const long long nbox = (long long)(d.x - 4) * (d.y - 4) * (d.z - 4) * (d.t - 4);
+  k_project_cells<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker,
+                                                          d, bx, (uint32_t)nbox, threshPhi,
+                                                          maxIter);
+}
+
+// knCvExpolBlur4d (optflow4d.cpp:613-626) fused with the preceding copy:
+// unmarked interior cells get avg of the 3^4 neighbourhood, scaled by the
+// double constant 1/81 and rounded back to float; others copy through.
+__global__ void __launch_bounds__(NT)
+k_expol_sweep(const float4 *__restrict__ in, float4 *__restrict__ out,
+              const float *__restrict__ mark, Dims4 d, BoxDecoder bx) {
+  const uint32_t n = (uint32_t)d.cells();
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(q, i, j, k, l);
+    if (!in_bounds(d, i, j, k, l, 1) || __ldg(mark + q) != 0.f) {
+      out[q] = __ldg(in + q);
+      continue;
+    }
+    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int vt = -1; vt <= 1; ++vt)
+      for (int zk = -1; zk <= 1; ++zk)
+        for (int yj = -1; yj <= 1; ++yj) {
+          const idx_t row = (idx_t)q + vt * sT + zk * sZ + yj * sY;
+#pragma unroll
+          for (int xi = -1; xi <= 1; ++xi) {
+            const float4 a = __ldg(in + row + xi);
+            val.x += a.x;
+            val.y += a.y;
+            val.z += a.z;
+            val.w += a.w;
+          }
+        }
+    const double c = 1. / 81.0;
+    out[q] = make_float4((float)((double)val.x * c), (float)((double)val.y * c),
+                         (float)((double)val.z * c), (float)((double)val.w * c));
+  }
+}
+
+void launch_expol_sweep(const float4 *in, float4 *out, const float *mark,
+                        Dims4 d, cudaStream_t s) {
+  BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
+  k_expol_sweep<<<grid_for(d.cells(), NT, 8), NT, 0, s>>>(in, out, mark, d, bx);
+}
+
+}  // namespace flof

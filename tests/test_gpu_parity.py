@@ -1,0 +1,362 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Per-cell stages are compared bit for bit: Grid4d ops, interpolation,
+advection, the direct Gaussian blur, the projection correction, the mode-2
+and mode-3 apply.  The PCG cannot be: its dot products are summed in a
+different order than the reference's serial loop, so solves are compared
+within the tolerance the reference's own float/double builds show
+(deformation 1e-4 relative L2, deformed SDF 1e-3 cells max-abs).
+"""
+import numpy as np
+import pytest
+
+import ofblend_gb300 as F
+from ofblend_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+REL_L2_DEFO = 1e-4     # deformation field, relative L2
+SDF_CELLS = 1e-3       # deformed SDF, max-abs in cells
+
+
+def grid_of(arr, ctx=None):
+    arr = np.ascontiguousarray(arr, dtype=np.float32)
+    if arr.ndim == 5:
+        T, Z, Y, X, _ = arr.shape
+        g = F.Grid4Vec4(dims=(X, Y, Z, T), ctx=ctx)
+    elif arr.ndim == 4:
+        T, Z, Y, X = arr.shape
+        g = F.Grid4Real(dims=(X, Y, Z, T), ctx=ctx)
+    else:
+        Z, Y, X = arr.shape
+        g = F.RealGrid(dims=(X, Y, Z, 1), ctx=ctx)
+    return g.from_numpy(arr)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def drop_pair(dims, a=0, b=1):
+    return synth.flow_input(synth.scene_for(a), dims), synth.flow_input(synth.scene_for(b), dims)
+
+
+# ---------------------------------------------------------------------------
+# Grid4d operations
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("nc", [1, 4])
+def test_grid_ops_bitexact(gpu, orc, nc):
+    r = np.random.default_rng(3)
+    shape = (7, 9, 10, 11) + ((4,) if nc == 4 else ())
+    a = r.standard_normal(shape).astype(np.float32)
+    b = r.standard_normal(shape).astype(np.float32)
+    ga, gb = grid_of(a), grid_of(b)
+    v4 = [0.3, -1.25, 2.5, 0.125]
+    c = v4 if nc == 4 else v4[0]
+    ga.addConst(c)
+    want = orc.addConst(a, c)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.multConst(c)
+    want = orc.multConst(want, c)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.addScaled(gb, c)
+    want = orc.addScaled(want, b, c)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.add(gb)
+    want = orc.add(want, b)
+    ga.sub(gb)
+    ga.sub(gb)
+    want = orc.sub(orc.sub(want, b), b)
+    assert np.array_equal(ga.to_numpy(), want)
+    assert np.float32(ga.getMax()) == np.float32(orc.getMax(want))
+    assert np.float32(ga.getMin()) == np.float32(orc.getMin(want))
+    assert np.float32(ga.getMaxAbs()) == np.float32(orc.getMaxAbs(want))
+    ga.setBound(c, 1)
+    want = orc.setBound(want, c, 1)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.setBoundNeumann(1)
+    want = orc.setBoundNeumann(want, 1)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.setBoundNeumann(0)
+    want = orc.setBoundNeumann(want, 0)
+    assert np.array_equal(ga.to_numpy(), want)
+    ga.setConst(c)
+    assert np.array_equal(ga.to_numpy(), orc.setConst(want, c))
+
+
+# ---------------------------------------------------------------------------
+# interpolation and advection
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("nc", [1, 4])
+@pytest.mark.parametrize("target,offset,scale", [
+    ((24, 20, 18, 14), (0, 0, 0, 0), (1, 1, 1, 1)),
+    ((6, 5, 5, 4), (0, 0, 0, 0), (1, 1, 1, 1)),
+    ((31, 17, 13, 9), (2.0, 1.5, 0.5, 3.0), (0.8, 0.8, 0.8, 1.0)),
+])
+def test_interpolate_bitexact(gpu, orc, nc, target, offset, scale):
+    r = np.random.default_rng(5)
+    shape = (8, 9, 10, 12) + ((4,) if nc == 4 else ())
+    src = r.standard_normal(shape).astype(np.float32)
+    gs = grid_of(src)
+    X, Y, Z, T = target
+    gt = (F.Grid4Vec4 if nc == 4 else F.Grid4Real)(dims=target)
+    (F.interpolateGrid4dVec if nc == 4 else F.interpolateGrid4d)(gt, gs, offset=offset, scale=scale)
+    want = orc.interpolateGrid4d(target, src, offset=offset, scale=scale)
+    assert np.array_equal(gt.to_numpy(), want)
+
+
+@pytest.mark.parametrize("nc", [1, 4])
+@pytest.mark.parametrize("dtFac", [1.0, 0.7, 0.25])
+def test_advect4d_bitexact(gpu, orc, nc, dtFac):
+    r = np.random.default_rng(11)
+    X, Y, Z, T = 19, 17, 13, 11
+    vel = r.uniform(-3.0, 3.0, size=(T, Z, Y, X, 4)).astype(np.float32)
+    src = r.standard_normal((T, Z, Y, X) + ((4,) if nc == 4 else ())).astype(np.float32)
+    gv, gs = grid_of(vel), grid_of(src)
+    F.advect4d(gv, gs, dtFac)
+    assert np.array_equal(gs.to_numpy(), orc.advect4d(vel, src, dtFac))
+
+
+# ---------------------------------------------------------------------------
+# blur, error metric
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("nc", [1, 4])
+@pytest.mark.parametrize("sigma", [2.0, 1.5, 1.125, 0.5])
+def test_gaussian_blur_bitexact(gpu, orc, nc, sigma):
+    r = np.random.default_rng(13)
+    a = r.standard_normal((9, 10, 11, 12) + ((4,) if nc == 4 else ())).astype(np.float32)
+    g = grid_of(a)
+    F.gaussianBlur4d(g, sigma, 1)
+    assert np.array_equal(g.to_numpy(), orc.gaussianBlur4d(a, sigma))
+
+
+@pytest.mark.parametrize("sigma", [2.0, 1.125])
+def test_gaussian_blur_separable_close(gpu, orc, sigma):
+    r = np.random.default_rng(17)
+    a = r.standard_normal((10, 11, 12, 13, 4)).astype(np.float32)
+    g = grid_of(a)
+    F.gaussianBlur4d(g, sigma, 2)
+    want = orc.gaussianBlur4d(a, sigma)
+    assert np.abs(g.to_numpy() - want).max() <= 2e-6 * max(1.0, np.abs(want).max())
+
+
+def test_calc_ls_diff(gpu, orc):
+    i0, i1 = drop_pair((20, 20, 20, 16))
+    g0, g1 = grid_of(i0), grid_of(i1)
+    out = F.Grid4Real(dims=(20, 20, 20, 16))
+    for corr, bnd in ((0.005, 3), (1.0, 0), (0.5, 1)):
+        got = F.calcLsDiff4d(g0, g1, out, corr, bnd)
+        want, wout = orc.calcLsDiff4d(i0, i1, corr, bnd, want_out=True)
+        # the double sum is taken in another order: equal up to one float ulp
+        assert abs(np.float32(got) - np.float32(want)) <= np.spacing(np.float32(want))
+        inner = (slice(bnd, 16 - bnd),) + (slice(bnd, 20 - bnd),) * 3
+        assert np.array_equal(out.to_numpy()[inner], wout[inner])
+
+
+# ---------------------------------------------------------------------------
+# solve
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("blur", [0.0, 4.0])
+def test_opticalflow4d_single_level(gpu, orc, blur):
+    dims = (24, 24, 24, 20)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    want, wit, wres = orc.opticalFlow4d(zv, i0, i1, 0.001, 0.0001, blur, 1e-4, 0.1)
+    gv = grid_of(zv)
+    it, res = F.opticalFlow4d(gv, grid_of(i0), grid_of(i1), wSmooth=0.001, wEnergy=0.0001,
+                              postVelBlur=blur, cgAccuracy=1e-4, resetBndWidth=0.1)
+    assert abs(it - wit) <= 2
+    assert res <= 1e-4
+    assert rel_l2(gv.to_numpy(), want) < REL_L2_DEFO
+
+
+def test_corrvelsof_bitexact(gpu, orc):
+    dims = (20, 20, 20, 16)
+    i0, i1 = drop_pair(dims)
+    r = np.random.default_rng(19)
+    vel = (r.standard_normal(i0.shape + (4,)) * 0.8).astype(np.float32)
+    want_vel, want_dst, _ = orc.corrVelsOf4d(vel, i0, i1, 4.0, 4.0, 0.1, 40)
+    gv, gd = grid_of(vel), F.Grid4Vec4(dims=dims)
+    F.corrVelsOf4d(gd, gv, grid_of(i0), None, grid_of(i1), 4.0, -9.0, 4.0, 0.1, 40)
+    assert np.array_equal(gv.to_numpy(), want_vel)
+    assert np.array_equal(gd.to_numpy(), want_dst)
+
+
+FLOF = dict(wSmooth=0.001, wEnergy=0.0001, cgAccuracy=0.01, postVelBlur=4, cfl=999, multiStep=3,
+            minGridSize=20, resetBndWidth=0.1)
+
+
+def _gpu_multiscale(i0, i1, **kw):
+    X = i0.shape[3]
+    dims = (i0.shape[3], i0.shape[2], i0.shape[1], i0.shape[0])
+    gv = F.Grid4Vec4(dims=dims)
+    err = F.opticalFlowMultiscale4d(gv, grid_of(i0), grid_of(i1), **kw)
+    return gv.to_numpy(), err, F.last_solve_stats()
+
+
+def test_multiscale_without_projection(gpu, orc):
+    dims = (32, 32, 32, 32)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    kw = dict(FLOF, doFinalProject=False)
+    want, werr, wst = orc.opticalFlowMultiscale4d(zv, i0, i1, **kw)
+    got, err, st = _gpu_multiscale(i0, i1, **kw)
+    assert [s[0] for s in st["solves"]] == [s[0] for s in wst]
+    assert rel_l2(got, want) < REL_L2_DEFO
+    assert abs(err - werr) <= 1e-3 * abs(werr)
+    # deformed SDF at alpha = 0.5, in cells (i / lsFactor)
+    sdf0 = i0 / synth.LS_FACTOR
+    a = orc.advect4d(want, sdf0, 0.5)
+    b = orc.advect4d(got, sdf0, 0.5)
+    assert np.abs(a - b).max() <= SDF_CELLS
+
+
+def test_multiscale_flof_defaults(gpu, orc):
+    """doFinalProject=True: the projection's line search and cut-off make
+    the result sensitive to last-bit differences of the PCG (the reference's
+    own float and double builds differ by O(1) relative L2 here), so the
+    check is on the error metric and the per-level solve structure."""
+    dims = (32, 32, 32, 32)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    kw = dict(FLOF, doFinalProject=True)
+    want, werr, wst = orc.opticalFlowMultiscale4d(zv, i0, i1, **kw)
+    got, err, st = _gpu_multiscale(i0, i1, **kw)
+    assert [s[0] for s in st["solves"]] == [s[0] for s in wst]
+    pre = orc.calcLsDiff4d(i0, i1, 0.1 / 20, 4)
+    assert err < pre and abs(err - werr) <= 0.05 * pre
+
+
+def test_golden_multiscale_fixture(gpu):
+    from conftest import ROOT
+    import os
+    g = np.load(os.path.join(ROOT, "tests", "golden", "flof_golden.npz"))
+    got, err, st = _gpu_multiscale(g["ms_i0"], g["ms_i1"], wSmooth=0.001, wEnergy=0.0001, cgAccuracy=0.01,
+                                   postVelBlur=4, cfl=999, multiStep=3, minGridSize=5,
+                                   doFinalProject=False, resetBndWidth=0.1)
+    # the fixture used the projection; the solve structure must still match
+    assert len(st["solves"]) == len(g["ms_iters"])
+    assert [s[1] for s in st["solves"]][:3] == list(g["ms_iters"][:3])
+
+
+# ---------------------------------------------------------------------------
+# applying a deformation (modes 2 and 3)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("twoway", [0, 1, 2])
+@pytest.mark.parametrize("alpha", [0.25, 0.5, 0.75])
+def test_deform4d_bitexact(gpu, orc, twoway, alpha):
+    r = np.random.default_rng(23)
+    dims = (18, 16, 14, 12)
+    X, Y, Z, T = dims
+    i0 = synth.sdf4d(synth.scene_for(0), dims)
+    i1 = synth.sdf4d(synth.scene_for(1), dims)
+    vel = r.uniform(-2, 2, size=(T, Z, Y, X, 4)).astype(np.float32)
+    vinv = r.uniform(-2, 2, size=(T, Z, Y, X, 4)).astype(np.float32)
+    out = F.Grid4Real(dims=dims)
+    F.deform4d(out, grid_of(i0), grid_of(i1), grid_of(vel), grid_of(vinv), alpha=alpha, twoway=twoway)
+    want = orc.deform4d(vel, vinv, i0, i1, np.float32(alpha), twoway=twoway)
+    assert np.array_equal(out.to_numpy(), want)
+
+
+def _optrun_case():
+    r = np.random.default_rng(29)
+    defo = r.uniform(-2.0, 2.0, size=(16, 16, 16, 16, 4)).astype(np.float32)
+    phi = synth.sdf4d(synth.scene_for(0), (48, 48, 48, 16))
+    return defo, phi
+
+
+@pytest.mark.parametrize("time,alpha,bord", [(3.5, 0.25, 4), (0.5, 1.0, 12), (15.5, 0.5, 1)])
+def test_optrun_bitexact(gpu, orc, time, alpha, bord):
+    defo, phi = _optrun_case()
+    dst0 = np.full((48, 48, 48), 0.5, np.float32)
+    want = orc.optRunFrame(defo, dst0, phi, time=time, blendAlpha=alpha, defoFactor=(3, 3, 3, 1),
+                           overrideSize=(48, 48, 48, 16), bordSkip=bord)
+    gd = grid_of(dst0)
+    gdef, gphi = grid_of(defo), grid_of(phi)
+    F.loadAdvectTimeSlice_OptInit(7, gdef, False, False, 0.2)
+    F.loadAdvectTimeSlice_OptRun(7, "defo", gd, gphi, time, alpha, 1.0, (0, 0, 0, 0), (1, 1, 1, 1),
+                                 (3, 3, 3, 1), overrideSize=(48, 48, 48, 16), bordSkip=bord)
+    F.loadAdvectTimeSlice_Finish(7)
+    assert np.array_equal(gd.to_numpy(), want)
+
+
+def test_optrun_twoway_blend(gpu, orc):
+    defo, phi = _optrun_case()
+    r = np.random.default_rng(31)
+    defo1 = r.uniform(-2.0, 2.0, size=defo.shape).astype(np.float32)
+    phi1 = synth.sdf4d(synth.scene_for(1), (48, 48, 48, 16))
+    alpha = 0.75
+    ai = np.float32(1.0 - alpha)
+    kw = dict(defoFactor=(3, 3, 3, 1), overrideSize=(48, 48, 48, 16), bordSkip=12)
+    d0 = orc.optRunFrame(defo, np.zeros((48, 48, 48), np.float32), phi, time=6.5, blendAlpha=alpha, **kw)
+    d1 = orc.optRunFrame(defo1, np.zeros((48, 48, 48), np.float32), phi1, time=6.5, blendAlpha=ai, **kw)
+    want = orc.addScaled(orc.multConst(d0[None], ai), d1[None], np.float32(alpha))[0]
+    gd = F.RealGrid(dims=(48, 48, 48, 1))
+    F.loadAdvectTimeSlice_OptInit(1, grid_of(defo))
+    F.loadAdvectTimeSlice_OptInit(2, grid_of(defo1))
+    gp0, gp1 = grid_of(phi), grid_of(phi1)
+    F.loadAdvectTimeSlice_OptRunTwoway(1, 2, gd, gp0, gp1, 6.5, alpha, 1.0, (0, 0, 0, 0), (1, 1, 1, 1),
+                                       (3, 3, 3, 1), overrideSize=(48, 48, 48, 16), bordSkip=12)
+    F.loadAdvectTimeSlice_Finish(1)
+    F.loadAdvectTimeSlice_Finish(2)
+    box = (slice(12, 36),) * 3
+    assert np.array_equal(gd.to_numpy()[box], want[box])
+
+
+def test_golden_fixtures_gpu(gpu):
+    from conftest import ROOT
+    import os
+    g = np.load(os.path.join(ROOT, "tests", "golden", "flof_golden.npz"))
+    gs = grid_of(g["adv_src"])
+    F.advect4d(grid_of(g["adv_vel"]), gs, 0.7)
+    assert np.array_equal(gs.to_numpy(), g["adv_out_a07"])
+    gsv = grid_of(g["adv_srcv"])
+    F.advect4d(grid_of(g["adv_vel"]), gsv, 1.0)
+    assert np.array_equal(gsv.to_numpy(), g["adv_outv_a1"])
+    gt = F.Grid4Real(dims=(13, 11, 10, 7))
+    F.interpolateGrid4d(gt, grid_of(g["ip_src"]), offset=(1.0, 0.5, 0.0, 2.0), scale=(0.8, 0.8, 0.8, 1.0))
+    assert np.array_equal(gt.to_numpy(), g["ip_up"])
+    gb = grid_of(g["blur_in"])
+    F.gaussianBlur4d(gb, 2.0)
+    assert np.array_equal(gb.to_numpy(), g["blur_s2"])
+    zv = np.zeros(g["of_i0"].shape + (4,), np.float32)
+    gv = grid_of(zv)
+    it, res = F.opticalFlow4d(gv, grid_of(g["of_i0"]), grid_of(g["of_i1"]), wSmooth=0.001, wEnergy=0.0001,
+                              postVelBlur=4.0, cgAccuracy=1e-4, resetBndWidth=0.1)
+    assert abs(it - int(g["of_iters"])) <= 2
+    assert rel_l2(gv.to_numpy(), g["of_vel"]) < REL_L2_DEFO
+    gd = grid_of(np.full((23, 22, 24), 7.0, np.float32))
+    F.loadAdvectTimeSlice_OptInit(3, grid_of(g["lk_defo"]))
+    F.loadAdvectTimeSlice_OptRun(3, "", gd, grid_of(g["lk_phi"]), 2.5, 0.25, 1.0, (0, 0, 0, 0), (1, 1, 1, 1),
+                                 (4, 4, 4, 1), overrideSize=(24, 22, 23, 5), bordSkip=2)
+    F.loadAdvectTimeSlice_Finish(3)
+    assert np.array_equal(gd.to_numpy(), g["lk_out"])
+
+
+# ---------------------------------------------------------------------------
+# failure behaviour (host-made failures only)
+# ---------------------------------------------------------------------------
+def test_errors_raise(gpu):
+    a = F.Grid4Real(dims=(8, 8, 8, 8))
+    b = F.Grid4Real(dims=(8, 8, 8, 9))
+    with pytest.raises(F.FlofError):
+        a.add(b)
+    with pytest.raises(F.FlofError):
+        F.advect4d(a, a)  # vel must be Vec4
+    d = F.RealGrid(dims=(30, 30, 30, 1))
+    with pytest.raises(F.FlofError) as e:
+        F.loadAdvectTimeSlice_OptRun(999, "", d, a, 0.5, 1.0, 1.0, 0, 1, 1)
+    assert e.value.status == 7
+
+
+def test_iteration_cap_is_reported_not_fatal(gpu):
+    dims = (16, 16, 16, 16)
+    i0, i1 = drop_pair(dims)
+    gv = F.Grid4Vec4(dims=dims)
+    F.opticalFlowMultiscale4d(gv, grid_of(i0), grid_of(i1), wSmooth=0.001, wEnergy=0.0001,
+                              cgAccuracy=1e-8, cgMaxIter=1, minGridSize=20)
+    st = F.last_solve_stats()
+    assert st["solves"][0][1] == 1 and st["solves"][0][3] == 4
+    assert np.isfinite(gv.to_numpy()).all()
