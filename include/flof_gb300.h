@@ -238,7 +238,8 @@ FLOF_API int flof_deform4d(flof_ctx *ctx, flof_grid *out, const flof_grid *i0,
 /* loadAdvectTimeSlice_OptInit (optflow4d.cpp:1871-1913).  The reference
  * names a .uni file that OptRun streams t-slices from; here the whole
  * deformation `defo` (Vec4 grid) is already resident in device memory and
- * the context keeps a reference to it until Finish.  Defo volumes
+ * the context pins it until Finish (a flof_grid_destroy in between is
+ * deferred until then).  Defo volumes
  * (useDefoVols, the three-data-set mode) are not supported: FLOF_E_ARG. */
 FLOF_API int flof_loadAdvectTimeSlice_OptInit(flof_ctx *ctx, int id,
                                               const flof_grid *defo,

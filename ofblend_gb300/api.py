@@ -431,7 +431,7 @@ def loadAdvectTimeSlice_OptInit(ID, fname1, useDefoVols=False, doAligned=False, 
     ctx = fname1.ctx
     check(ctx.lib.flof_loadAdvectTimeSlice_OptInit(ctx.h, int(ID), fname1.h, int(bool(useDefoVols)),
                                                    int(bool(doAligned)), float(partialLoadFac)))
-    _lats_ctx[int(ID)] = ctx
+    _lats_ctx[int(ID)] = (ctx, fname1)  # keeps the deformation grid alive until Finish
 
 
 _lats_ctx: dict = {}
@@ -468,7 +468,8 @@ def loadAdvectTimeSlice_OptRunTwoway(ID0, ID1, dst, phi0, phi1, time, blendAlpha
 
 def loadAdvectTimeSlice_Finish(ID):
     """loadAdvectTimeSlice_Finish (optflow4d.cpp:1930-1950)."""
-    ctx = _lats_ctx.pop(int(ID), None)
-    if ctx is None:
+    ent = _lats_ctx.pop(int(ID), None)
+    if ent is None:
         return
+    ctx = ent[0]
     check(ctx.lib.flof_loadAdvectTimeSlice_Finish(ctx.h, int(ID)))

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflof_gb300.so")
-SOURCES = ["flof_ops.cu", "flof_solve.cu", "flof_host.cu"]
+SOURCES = ["flof_ops.cu", "flof_solve.cu", "flof_stencil.cu", "flof_host.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -32,6 +32,9 @@ def flags() -> list[str]:
     return ARCH + [
         "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
         "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+        # host-side parameter arithmetic (grid factors, slice times) must not
+        # be contracted to FMA either: GCC does so by default on aarch64
+        "-Xcompiler", "-ffp-contract=off",
         "-Xptxas", "-warn-spills",
         "-I", CSRC, "-I", os.path.join(os.path.dirname(HERE), "include"),
     ]

@@ -141,6 +141,7 @@ struct flof_ctx {
   flof_solve_stats *stats = nullptr;
   int cfl_sync = 1;
   int profiling = 0;
+  std::map<std::pair<uint32_t, int>, float *> wsum_cache;  // (sigma bits, radius)
   std::vector<ProfRec> recs;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
@@ -152,6 +153,10 @@ struct flof_grid {
   int elem = FLOF_REAL;
   void *d = nullptr;
   bool owned = false;
+  // OptInit pins the deformation grid it reads from; destroying a pinned
+  // grid is deferred until the last Finish releases it.
+  int pins = 0;
+  bool destroy_pending = false;
   Dims4 D() const { return Dims4{dims[0], dims[1], dims[2], dims[3]}; }
   int nc() const { return elem == FLOF_VEC4 ? 4 : 1; }
   long long cells() const { return (long long)dims[0] * dims[1] * dims[2] * dims[3]; }
@@ -159,6 +164,21 @@ struct flof_grid {
   float *f() const { return (float *)d; }
   float4 *v() const { return (float4 *)d; }
 };
+
+static void grid_free(flof_grid *g) {
+  if (g->owned && g->d) {
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    cudaFree(g->d);
+  }
+  delete g;
+}
+
+static void grid_unpin(flof_grid *g) {
+  if (!g) return;
+  if (g->pins > 0) g->pins--;
+  if (g->pins == 0 && g->destroy_pending) grid_free(g);
+}
 
 namespace {
 
@@ -326,6 +346,39 @@ float ls_diff(flof_ctx *c, const float *i0, const float *i1, float *out, Dims4 d
   return read_f(c, c->fres + 1);
 }
 
+// In-bounds weight sums of knGaussianBlur by clipping pattern: per axis the
+// number of taps cut below 0 and above size-1; summed in the reference's tap
+// order (t, z, y, x), skipping the cut taps.
+const float *wsum_table(flof_ctx *c, float sigma, int s, const float *wtab) {
+  uint32_t bits;
+  memcpy(&bits, &sigma, sizeof(bits));
+  auto key = std::make_pair(bits, s);
+  auto it = c->wsum_cache.find(key);
+  if (it != c->wsum_cache.end()) return it->second;
+  const int P = s + 1, P1 = P * P;
+  std::vector<float> h((size_t)P1 * P1 * P1 * P1);
+  for (int ct = 0; ct < P1; ++ct)
+    for (int cz = 0; cz < P1; ++cz)
+      for (int cy = 0; cy < P1; ++cy)
+        for (int cx = 0; cx < P1; ++cx) {
+          const int lo_t = -s + ct / P, hi_t = s - ct % P;
+          const int lo_z = -s + cz / P, hi_z = s - cz % P;
+          const int lo_y = -s + cy / P, hi_y = s - cy % P;
+          const int lo_x = -s + cx / P, hi_x = s - cx % P;
+          float w = 0.f;
+          for (int vt = lo_t; vt <= hi_t; ++vt)
+            for (int zk = lo_z; zk <= hi_z; ++zk)
+              for (int yj = lo_y; yj <= hi_y; ++yj)
+                for (int xi = lo_x; xi <= hi_x; ++xi) w += wtab[vt * vt + zk * zk + yj * yj + xi * xi];
+          h[((size_t)(ct * P1 + cz) * P1 + cy) * P1 + cx] = w;
+        }
+  float *dptr = nullptr;
+  CK(cudaMalloc(&dptr, h.size() * sizeof(float)));
+  CK(cudaMemcpy(dptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  c->wsum_cache[key] = dptr;
+  return dptr;
+}
+
 // gaussianBlurGeneric(a, sigma, iter = 1) (optflow4d.cpp:160-174).
 void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurType) {
   int s = trunc_d(1. * (double)sigma + 0.5);
@@ -339,10 +392,18 @@ void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurTyp
     DBuf tmp(c, nb);
     // pass 1: a -> fresh tmp (zero ring); pass 2: tmp -> a (ring keeps the
     // original values): the state after the reference's two swaps.
-    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
-        launch_gauss_pass(a, tmp.f(), d, nc, s, wtab, 1, c->stream));
-    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
-        launch_gauss_pass(tmp.f(), a, d, nc, s, wtab, 0, c->stream));
+    if (gauss_slab_supported(s, d)) {
+      const float *ws = wsum_table(c, sigma, s, wtab);
+      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+          launch_gauss_slab(a, tmp.f(), d, nc, s, wtab, ws, 1, c->stream));
+      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+          launch_gauss_slab(tmp.f(), a, d, nc, s, wtab, ws, 0, c->stream));
+    } else {
+      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+          launch_gauss_pass(a, tmp.f(), d, nc, s, wtab, 1, c->stream));
+      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+          launch_gauss_pass(tmp.f(), a, d, nc, s, wtab, 0, c->stream));
+    }
   } else {
     float w1[8];
     for (int q = 0; q <= s; ++q)
@@ -464,7 +525,7 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
         launch_project_cells(dst, vel, phiOrg, phiTarget, marker.f(), d, threshPhi, maxIter,
                                c->stream));
     for (int s = 0; s < doCvExtrapol; ++s) {
-      KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_sweep(A, B, marker.f(), d, c->stream));
+      KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_slab(A, B, marker.f(), d, c->stream));
       float4 *sw = A;
       A = B;
       B = sw;
@@ -772,8 +833,10 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   if (!c) return FLOF_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  for (auto &kv : c->lats)
+  for (auto &kv : c->lats) {
     if (kv.second.vt) c->pool.put(kv.second.vt);
+    if (kv.second.defo) grid_unpin(const_cast<flof_grid *>(kv.second.defo));
+  }
   c->lats.clear();
   c->pool.release_all();
   cudaFree(c->st);
@@ -786,6 +849,7 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   cudaFreeHost(c->fres_h);
   cudaFreeHost(c->dres_h);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  for (auto &kv : c->wsum_cache) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return FLOF_OK;
@@ -912,6 +976,10 @@ FLOF_API int flof_grid_wrap(flof_ctx *c, const int dims[4], int elem, void *ptr,
 
 FLOF_API int flof_grid_destroy(flof_grid *g) {
   if (!g) return FLOF_OK;
+  if (g->pins > 0) {
+    g->destroy_pending = true;
+    return FLOF_OK;
+  }
   if (g->owned && g->d) {
     cudaSetDevice(g->ctx->device);
     cudaStreamSynchronize(g->ctx->stream);
@@ -1344,6 +1412,8 @@ FLOF_API int flof_loadAdvectTimeSlice_OptInit(flof_ctx *c, int id, const flof_gr
     set_ctx_device(c);
     LatsData &L = c->lats[id];
     if (L.vt) c->pool.put(L.vt);
+    if (L.defo) grid_unpin(const_cast<flof_grid *>(L.defo));
+    const_cast<flof_grid *>(defo)->pins++;
     L.defo = defo;
     L.vt = c->pool.get((size_t)defo->dims[0] * defo->dims[1] * defo->dims[2] * sizeof(float4));
     L.lastT = -1;
@@ -1357,6 +1427,7 @@ FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *c, int id) {
     if (it == c->lats.end()) return;
     CK(cudaStreamSynchronize(c->stream));
     if (it->second.vt) c->pool.put(it->second.vt);
+    if (it->second.defo) grid_unpin(const_cast<flof_grid *>(it->second.defo));
     c->lats.erase(it);
   });
 }

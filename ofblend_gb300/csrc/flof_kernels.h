@@ -136,6 +136,17 @@ void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
                            int axis, int s, const float *w1d, int border_mode,
                            cudaStream_t st);
 
+// Shared-memory slab versions (flof_stencil.cu) of the blur pass for radius
+// 1 and 2 and of the extrapolation sweep; same results bit for bit.
+// wsum_dev holds the in-bounds weight sums by clipping pattern
+// ((S+1)^2 codes per axis, t-major).
+bool gauss_slab_supported(int s, Dims4 d);
+void launch_gauss_slab(const float *src, float *dst, Dims4 d, int nc, int s,
+                       const float *wtab, const float *wsum_dev, int zero_border,
+                       cudaStream_t st);
+void launch_expol_slab(const float4 *in, float4 *out, const float *mark, Dims4 d,
+                       cudaStream_t st);
+
 // ---- projection correction ------------------------------------------------------
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,
