@@ -242,6 +242,52 @@ __device__ __forceinline__ float4 interp3_vec(const float4 *__restrict__ data,
   return r;
 }
 
+// ---- compensated accumulation ------------------------------------------------
+
+// Float-float accumulator (Knuth's TwoSum): `hi` carries the running sum,
+// `lo` the exact rounding errors of the adds.  Accumulating float products
+// this way is about as accurate as the reference's double accumulator
+// (optflow4d.cpp:234-241) and costs FP32 adds only; GB300's FP64 rate is a
+// small fraction of its FP32 rate.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF &a, float p) {
+  const float s = a.hi + p;
+  const float bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (p - bp);
+  a.hi = s;
+  a.lo += e;
+}
+__device__ __forceinline__ double ff_value(const FF &a) { return (double)a.hi + (double)a.lo; }
+
+// (float)((double)v * (1./81.)) as the reference computes it
+// (knCvExpolBlur4d, optflow4d.cpp:625), mostly without FP64 work.  With
+// c = c_hi + c_lo (+ a remainder below 2^-48 c), p + lo approximates v*c to
+// about 2^-46 relative and f = RN(p + lo).  Rounding the exact product to
+// double and then to float gives f unless the product lies within 2^-53 of
+// a float rounding midpoint; products within 2^-40 of a midpoint, and tiny
+// or non-finite values, take the double path.
+__device__ __forceinline__ float mul_inv81(float v) {
+  constexpr double c = 1. / 81.0;
+  constexpr float c_hi = (float)c;
+  constexpr float c_lo = (float)(c - (double)c_hi);
+  const float p = v * c_hi;
+  const float pe = __fmaf_rn(v, c_hi, -p);  // v*c_hi - p, exact
+  const float lo = __fmaf_rn(v, c_lo, pe);
+  const float f = p + lo;
+  const unsigned E = (__float_as_uint(f) >> 23) & 0xffu;
+  if (E > 41u && E < 255u) {
+    const float rem = (p - f) + lo;                       // ~ v*c - f
+    const float half_ulp = __uint_as_float((E - 24u) << 23);
+    const float margin = __uint_as_float((E - 40u) << 23);
+    if (fabsf(fabsf(rem) - half_ulp) > margin) return f;
+  } else if (v == 0.f) {
+    return f;
+  }
+  return (float)((double)v * c);
+}
+
 // ---- reductions -----------------------------------------------------------
 
 __device__ __forceinline__ double warp_sum(double v) {

@@ -55,7 +55,7 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
                    float *fpart) {
   __shared__ double shd[NT / 32];
   __shared__ float shf[NT / 32];
-  double dot = 0.0;
+  FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -105,13 +105,13 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
     g[id] = gg;
     r[id] = rr;
     p[id] = z;
-    dot += (double)(z.x * rr.x);
-    dot += (double)(z.y * rr.y);
-    dot += (double)(z.z * rr.z);
-    dot += (double)(z.w * rr.w);
+    ff_add(dot, z.x * rr.x);
+    ff_add(dot, z.y * rr.y);
+    ff_add(dot, z.z * rr.z);
+    ff_add(dot, z.w * rr.w);
     mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
   }
-  const double bd = block_sum<NT>(dot, shd);
+  const double bd = block_sum<NT>(ff_value(dot), shd);
   const float bm = block_max<NT>(mx, shf);
   if (threadIdx.x == 0) {
     dpart[blockIdx.x] = bd;
@@ -167,7 +167,7 @@ k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
             OFConsts c, CGState *st, double *dpart) {
   if (st->done) return;
   __shared__ double shd[NT / 32];
-  double dot = 0.0;
+  FF dot = {0.f, 0.f};
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   const float o = c.offd;
   for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
@@ -203,12 +203,12 @@ k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
     }
     const float4 qq = make_float4(vv[0], vv[1], vv[2], vv[3]);
     q[id] = qq;
-    dot += (double)(pc.x * qq.x);
-    dot += (double)(pc.y * qq.y);
-    dot += (double)(pc.z * qq.z);
-    dot += (double)(pc.w * qq.w);
+    ff_add(dot, pc.x * qq.x);
+    ff_add(dot, pc.y * qq.y);
+    ff_add(dot, pc.z * qq.z);
+    ff_add(dot, pc.w * qq.w);
   }
-  const double bd = block_sum<NT>(dot, shd);
+  const double bd = block_sum<NT>(ff_value(dot), shd);
   if (threadIdx.x == 0) dpart[blockIdx.x] = bd;
   if (last_block_arrives(&st->counter[1])) {
     double s = 0.0;
@@ -239,7 +239,7 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
   __shared__ double shd[NT / 32];
   __shared__ float shf[NT / 32];
   const float a = (float)st->alpha;
-  double dot = 0.0;
+  FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
   for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
        n += gridDim.x * blockDim.x) {
@@ -259,13 +259,13 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
     x[id] = xx;
     r[id] = rr;
     const float4 pre = precond_of(gg, c.diag);
-    dot += (double)((rr.x * pre.x) * rr.x);
-    dot += (double)((rr.y * pre.y) * rr.y);
-    dot += (double)((rr.z * pre.z) * rr.z);
-    dot += (double)((rr.w * pre.w) * rr.w);
+    ff_add(dot, (rr.x * pre.x) * rr.x);
+    ff_add(dot, (rr.y * pre.y) * rr.y);
+    ff_add(dot, (rr.z * pre.z) * rr.z);
+    ff_add(dot, (rr.w * pre.w) * rr.w);
     mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
   }
-  const double bd = block_sum<NT>(dot, shd);
+  const double bd = block_sum<NT>(ff_value(dot), shd);
   const float bm = block_max<NT>(mx, shf);
   if (threadIdx.x == 0) {
     dpart[blockIdx.x] = bd;
@@ -620,9 +620,7 @@ k_expol_sweep(const float4 *__restrict__ in, float4 *__restrict__ out,
             val.w += a.w;
           }
         }
-    const double c = 1. / 81.0;
-    out[q] = make_float4((float)((double)val.x * c), (float)((double)val.y * c),
-                         (float)((double)val.z * c), (float)((double)val.w * c));
+    out[q] = make_float4(mul_inv81(val.x), mul_inv81(val.y), mul_inv81(val.z), mul_inv81(val.w));
   }
 }
 

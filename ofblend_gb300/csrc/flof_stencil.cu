@@ -135,7 +135,6 @@ k_slab_stencil(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, 
   for (int q = 0; q < RY; ++q)
 #pragma unroll
     for (int r = 0; r < RX; ++r) val[q][r] = VT<NC>::zero();
-  T centre[RY][RX];
 
   constexpr int K = 2 * S + 1;
   constexpr int NP = K * K;  // (t, z) offsets
@@ -177,10 +176,6 @@ k_slab_stencil(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, 
           for (int r = 0; r < RX; ++r)
 #pragma unroll
             for (int xi = -S; xi <= S; ++xi) acc(val[q][r], a[r + S + xi]);
-        }
-        if (vt == 0 && zk == 0 && yj == 0) {
-#pragma unroll
-          for (int r = 0; r < RX; ++r) centre[q][r] = a[r + S];
         }
       }
     }
@@ -224,19 +219,18 @@ k_slab_stencil(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, 
         out[id] = v;
       } else {
         if (!inner || __ldg(mark + id) != 0.f) {
-          out[id] = centre[q][r];
+          out[id] = __ldg((const T *)src + id);
           continue;
         }
-        const double c81 = 1. / 81.0;
         T v = val[q][r];
         if (NC == 4) {
           float4 &f = *(float4 *)&v;
-          f.x = (float)((double)f.x * c81);
-          f.y = (float)((double)f.y * c81);
-          f.z = (float)((double)f.z * c81);
-          f.w = (float)((double)f.w * c81);
+          f.x = mul_inv81(f.x);
+          f.y = mul_inv81(f.y);
+          f.z = mul_inv81(f.z);
+          f.w = mul_inv81(f.w);
         } else {
-          *(float *)&v = (float)((double)(*(float *)&v) * c81);
+          *(float *)&v = mul_inv81(*(float *)&v);
         }
         out[id] = v;
       }
