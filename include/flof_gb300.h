@@ -235,6 +235,26 @@ FLOF_API int flof_deform4d(flof_ctx *ctx, flof_grid *out, const flof_grid *i0,
                            const flof_grid *velInv, float alpha,
                            float alphaInv, int twoway);
 
+/* calcLsDiff4d without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that cannot allocate
+ * device memory where they need the error metric: code recorded into a CUDA
+ * graph by stream capture (allocation cannot be captured) and applications
+ * that reserve all device memory at start-up.  It computes the same value
+ * as flof_calcLsDiff4d (calcLsDiffTempl, optflow4d.cpp:895-927) from the
+ * caller's device buffers on the caller's stream (void* cudaStream_t, NULL
+ * for the legacy default stream) and writes it to the device float
+ * `result`; `out` (device, nullable) receives the per-cell values.
+ * Grids up to 2^31-1 cells; larger ones are rejected with FLOF_E_ARG.
+ * Its scratch is a fixed 8 KiB device array in the library (1024 block
+ * partials plus a counter), held by every GPU that loads the library until
+ * exit and shared by all calls: calls that overlap on the GPU race on it.
+ * The first call on a device looks the array's address up; make that first
+ * call before any stream capture. */
+FLOF_API int flof_calcLsDiff4d_noalloc(const float *i0, const float *i1,
+                                       float *out, const int dims[4],
+                                       float correction, int bnd,
+                                       float *result, void *stream);
+
 /* loadAdvectTimeSlice_OptInit (optflow4d.cpp:1871-1913).  The reference
  * names a .uni file that OptRun streams t-slices from; here the whole
  * deformation `defo` (Vec4 grid) is already resident in device memory and

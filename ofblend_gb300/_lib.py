@@ -118,6 +118,7 @@ SIGNATURES = {
     "flof_gaussianBlur4d": (I, [P, P, F, I]),
     "flof_advect4d": (I, [P, P, P, F]),
     "flof_calcLsDiff4d": (I, [P, P, P, P, F, I, FP]),
+    "flof_calcLsDiff4d_noalloc": (I, [P, P, P, P, F, I, P, P]),
     "flof_interpolateGrid4d": (I, [P, P, P, P, P, P]),
     "flof_interpolateGrid4dVec": (I, [P, P, P, P, P, P]),
     "flof_deform4d": (I, [P, P, P, P, P, P, F, F, I]),

@@ -738,6 +738,10 @@ void grid_factor4d(const float s1[4], const float s2in[4], const float optSize[4
 
 }  // namespace
 
+namespace flof {
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+}  // namespace flof
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

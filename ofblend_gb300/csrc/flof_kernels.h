@@ -10,6 +10,9 @@
 
 namespace flof {
 
+// Sets the thread-local message returned by flof_last_error().
+void set_last_error(const char *msg);
+
 // Number of SMs of the current device (cached), used to size grids.
 int sm_count();
 // Blocks for a grid-stride launch over n items with `nt` threads per block.
