@@ -128,6 +128,13 @@ FLOF_API int flof_ctx_profile_count(flof_ctx *ctx, int *n);
 FLOF_API int flof_ctx_profile_record(flof_ctx *ctx, int i, int *cls,
                                      int *size_x, double *bytes, float *ms);
 FLOF_API const char *flof_kernel_class_name(int cls);
+/* Context options (flof_ctx_set_option).
+ * FLOF_OPT_CFL_SYNC: 0 (default) the CFL substep count of advectCflHelper4d
+ *   (optflow4d.cpp:1309-1321) is checked on the device and a call that needs
+ *   more than one substep is redone; 1 the host reads max |v| before every
+ *   CFL-guarded advection. */
+enum { FLOF_OPT_CFL_SYNC = 2 };
+FLOF_API int flof_ctx_set_option(flof_ctx *ctx, int option, int value);
 /* Release cached device buffers of the context's pool. */
 FLOF_API int flof_ctx_trim(flof_ctx *ctx);
 

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(_HERE, "libflof_gb300.so")
 
 FLOF_REAL = 1
 FLOF_VEC4 = 8
+FLOF_OPT_CFL_SYNC = 2
 MAX_SOLVE_STATS = 64
 
 STATUS = {
@@ -88,6 +89,7 @@ SIGNATURES = {
     "flof_ctx_stream": (P, [P]),
     "flof_ctx_kernel_launches": (ctypes.c_longlong, [P]),
     "flof_ctx_trim": (I, [P]),
+    "flof_ctx_set_option": (I, [P, I, I]),
     "flof_ctx_profile": (I, [P, I]),
     "flof_ctx_profile_count": (I, [P, IP]),
     "flof_ctx_profile_record": (I, [P, I, IP, IP, ctypes.POINTER(ctypes.c_double), FP]),

@@ -94,6 +94,10 @@ class Context:
     def trim(self):
         check(self.lib.flof_ctx_trim(self.h))
 
+    def set_option(self, option: int, value: int):
+        """flof_ctx_set_option, e.g. _lib.FLOF_OPT_CFL_SYNC."""
+        check(self.lib.flof_ctx_set_option(self.h, int(option), int(value)))
+
     def profile(self, enable: bool = True):
         """Start (clearing old records) or stop per-launch event tracing."""
         check(self.lib.flof_ctx_profile(self.h, int(bool(enable))))

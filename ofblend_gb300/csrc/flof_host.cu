@@ -139,7 +139,11 @@ struct flof_ctx {
   int syncs = 0;
   std::map<int, LatsData> lats;
   flof_solve_stats *stats = nullptr;
-  int cfl_sync = 1;
+  // 0: CFL substep counts are checked on the device (one substep assumed,
+  // exceptions flagged in cfl_flag); 1: the host reads max |v| each time.
+  int cfl_sync = 0;
+  int *cfl_flag = nullptr;
+  int cfl_force_sync = 0;
   int profiling = 0;
   std::map<std::pair<uint32_t, int>, float *> wsum_cache;  // (sigma bits, radius)
   std::vector<ProfRec> recs;
@@ -317,6 +321,17 @@ float vec_max_norm(flof_ctx *c, const float4 *v, Dims4 d) {
 // advectCflHelper4d (:1309-1321) with the solver dt = 1 and velFactor = 1
 // (a multiplication by 1 is exact, so the velocity copy is skipped).
 void advect_cfl(flof_ctx *c, Dims4 d, float cfl, const float4 *vel, float *grid, int nc) {
+  if (!c->cfl_sync) {
+    KLP(c, KC_REDUCE, d.x, d.cells() * 16,
+        launch_reduce_minmax((const float *)vel, d.cells(), 4, 0, c->fpart, c->counter + 4,
+                             c->fres + 0, c->stream));
+    DBuf tmp(c, (size_t)d.cells() * nc * sizeof(float));
+    KLP(c, KC_ADVECT, d.x, d.cells() * (16 + 8 * nc),
+        launch_advect_cfl1(vel, grid, tmp.f(), d, nc, c->fres + 0, cfl, c->cfl_flag, c->stream));
+    CK(cudaMemcpyAsync(grid, tmp.p, (size_t)d.cells() * nc * sizeof(float),
+                       cudaMemcpyDeviceToDevice, c->stream));
+    return;
+  }
   const float orgDt = 1.0f;
   const float maxVel = vec_max_norm(c, vel, d) * orgDt;
   const int steps = trunc_f(maxVel / cfl) + 1;
@@ -448,37 +463,38 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
   KLP(c, KC_ASSEMBLE, d.x, nint(d) * 8 + d.cells() * 64,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
+  // Iterations are launched in chunks without waiting; every kernel returns
+  // at once when the state says done.  After each chunk the host reads the
+  // state and sizes the next chunk from the observed reduction rate.
   int it = 0;
   int chunk = 4;
   for (;;) {
-    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
-    sync(c);
-    if (c->st_h->done != CG_RUNNING) break;
-    if (it >= a.cgMaxIter) break;
-    // Estimate the remaining iterations from the observed reduction rate.
-    if (it > 0) {
-      const double ratio = (double)c->st_h->resMax / c->st_h->resIni;
-      const double target = c->st_h->acc / c->st_h->resIni;
-      if (ratio > 0 && ratio < 1 && target > 0) {
-        const double rate = log(ratio) / it;
-        double est = rate < 0 ? (log(target) - log(ratio)) / rate : 64;
-        int e = (int)(est * 1.1) + 2;
-        chunk = e < 2 ? 2 : (e > 64 ? 64 : e);
-      } else {
-        chunk = chunk * 2 > 64 ? 64 : chunk * 2;
-      }
-    }
     const int n = (a.cgMaxIter - it) < chunk ? (a.cgMaxIter - it) : chunk;
     for (int s = 0; s < n; ++s) {
+      const int kk = it + s;
       KLP(c, KC_MATVEC, d.x, nint(d) * 48,
           launch_cg_matvec(p.v(), g.v(), q.v(), d, k, c->st, c->dpart, c->stream));
       KLP(c, KC_UPDATE, d.x, nint(d) * 112,
           launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, c->st, c->dpart,
-                             c->fpart, it + s, a.cgMaxIter, c->stream));
+                           c->fpart, kk, a.cgMaxIter, c->stream));
       KLP(c, KC_DIRECTION, d.x, nint(d) * 64,
           launch_cg_direction(p.v(), r.v(), g.v(), d, k, c->st, c->stream));
     }
     it += n;
+    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (c->st_h->done != CG_RUNNING) break;
+    if (it >= a.cgMaxIter) break;
+    const double ratio = (double)c->st_h->resMax / c->st_h->resIni;
+    const double target = c->st_h->acc / c->st_h->resIni;
+    if (ratio > 0 && ratio < 1 && target > 0) {
+      const double rate = log(ratio) / it;
+      const double est = rate < 0 ? (log(target) - log(ratio)) / rate : 64;
+      const int e = (int)(est * 1.1) + 2;
+      chunk = e < 2 ? 2 : (e > 64 ? 64 : e);
+    } else {
+      chunk = chunk * 2 > 64 ? 64 : chunk * 2;
+    }
   }
   int status = c->st_h->done;
   if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
@@ -812,12 +828,14 @@ FLOF_API int flof_ctx_create(int device, flof_ctx **out) {
     try {
       CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
       c->stream = c->own_stream;
-      const int maxBlocks = sm_count() * 16 + 64;
+      const int maxBlocks = 65536;
       CK(cudaMalloc(&c->st, sizeof(CGState)));
       CK(cudaMemset(c->st, 0, sizeof(CGState)));
       CK(cudaMallocHost(&c->st_h, sizeof(CGState)));
       CK(cudaMalloc(&c->dpart, sizeof(double) * maxBlocks));
       CK(cudaMalloc(&c->fpart, sizeof(float) * maxBlocks));
+      CK(cudaMalloc(&c->cfl_flag, sizeof(int)));
+      CK(cudaMemset(c->cfl_flag, 0, sizeof(int)));
       CK(cudaMalloc(&c->counter, sizeof(unsigned int) * 8));
       CK(cudaMemset(c->counter, 0, sizeof(unsigned int) * 8));
       CK(cudaMalloc(&c->fres, sizeof(float) * 16));
@@ -848,6 +866,7 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   cudaFree(c->dpart);
   cudaFree(c->fpart);
   cudaFree(c->counter);
+  cudaFree(c->cfl_flag);
   cudaFree(c->fres);
   cudaFree(c->dres);
   cudaFreeHost(c->fres_h);
@@ -916,6 +935,18 @@ FLOF_API int flof_ctx_profile_record(flof_ctx *c, int i, int *cls, int *size_x, 
 FLOF_API const char *flof_kernel_class_name(int cls) {
   if (cls < 0 || cls >= KC_COUNT) return "unknown";
   return kc_names[cls];
+}
+
+FLOF_API int flof_ctx_set_option(flof_ctx *c, int option, int value) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    if (option == FLOF_OPT_CFL_SYNC) {
+      need(value == 0 || value == 1, "FLOF_OPT_CFL_SYNC takes 0 or 1");
+      c->cfl_force_sync = value;
+    } else {
+      fail(FLOF_E_ARG, "unknown context option");
+    }
+  });
 }
 
 FLOF_API int flof_ctx_trim(flof_ctx *c) {
@@ -1189,10 +1220,30 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     m.cgMaxIter = pp.cgMaxIter;
     float e;
     try {
+      // speculative pass: CFL substep counts checked on the device
+      DBuf vel_in(c, vel->bytes());
+      CK(cudaMemcpyAsync(vel_in.p, vel->d, vel->bytes(), cudaMemcpyDeviceToDevice, c->stream));
+      CK(cudaMemsetAsync(c->cfl_flag, 0, sizeof(int), c->stream));
+      c->cfl_sync = c->cfl_force_sync;
       e = multiscale(c, vel->D(), vel->v(), i0->f(), i1->f(), m, pp.level);
+      int flag = 0;
+      CK(cudaMemcpyAsync(c->fres_h + 8, c->cfl_flag, sizeof(int), cudaMemcpyDeviceToHost,
+                         c->stream));
       CK(cudaStreamSynchronize(c->stream));
+      memcpy(&flag, c->fres_h + 8, sizeof(int));
+      if (flag) {
+        // some advection needed more than one CFL substep: redo the call
+        // with host-side substep counts
+        memset(&local, 0, sizeof(local));
+        CK(cudaMemcpyAsync(vel->d, vel_in.p, vel->bytes(), cudaMemcpyDeviceToDevice, c->stream));
+        c->cfl_sync = 1;
+        e = multiscale(c, vel->D(), vel->v(), i0->f(), i1->f(), m, pp.level);
+        c->cfl_sync = 0;
+        CK(cudaStreamSynchronize(c->stream));
+      }
     } catch (...) {
       c->stats = nullptr;
+      c->cfl_sync = 0;
       throw;
     }
     c->stats = nullptr;

@@ -55,6 +55,11 @@ void launch_resample(float *target, Dims4 td, const float *source, Dims4 sd,
 // border ring of dst is written with zeros.
 void launch_advect(const float4 *vel, const float *src, float *dst, Dims4 d,
                    int nc, float dt, cudaStream_t s);
+// One substep of the CFL-guarded advection with the substep count checked
+// on the device: maxn2 is the device max |v|^2; *flag is set when
+// int(maxVel/cfl)+1 != 1.
+void launch_advect_cfl1(const float4 *vel, const float *src, float *dst, Dims4 d, int nc,
+                        const float *maxn2, float cfl, int *flag, cudaStream_t s);
 // Two-way blend of deform4d (scenes/flof.py:603-610) in one pass:
 // out = (advect(vel,i0,a) * (1-a)) + a * advect(velInv,i1,1-a).
 void launch_deform_twoway(const float4 *vel, const float4 *velInv,

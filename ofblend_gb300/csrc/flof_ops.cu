@@ -348,9 +348,20 @@ void launch_resample(float *target, Dims4 td, const float *source, Dims4 sd,
 // bnd=1 cells of a fresh (zeroed) grid.
 // ---------------------------------------------------------------------------
 
+// With `maxn2` set, the launch is the single substep of advectCflHelper4d
+// (optflow4d.cpp:1309-1321): the substep count int(maxVel/cfl)+1 is
+// evaluated here from the device-resident max |v|^2, and a count other than
+// one is reported through `flag` so that the host can redo the call with
+// host-side substeps.
 template <int NC>
 __global__ void k_advect(const float4 *__restrict__ vel, const float *__restrict__ src,
-                         float *__restrict__ dst, Dims4 d, BoxDecoder bx, float dt) {
+                         float *__restrict__ dst, Dims4 d, BoxDecoder bx, float dt,
+                         const float *maxn2, float cfl, int *flag) {
+  if (maxn2 && blockIdx.x == 0 && threadIdx.x == 0) {
+    const float maxVel = sqrtf(*maxn2) * 1.0f;
+    const int steps = trunc_i(maxVel / cfl) + 1;
+    if (steps != 1) *flag = 1;
+  }
   const uint32_t n = (uint32_t)d.cells();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n;
        q += gridDim.x * blockDim.x) {
@@ -377,9 +388,20 @@ void launch_advect(const float4 *vel, const float *src, float *dst, Dims4 d,
   BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
   const int nb = grid_for(d.cells(), NT);
   if (nc == 4)
-    k_advect<4><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt);
+    k_advect<4><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt, nullptr, 0.f, nullptr);
   else
-    k_advect<1><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt);
+    k_advect<1><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt, nullptr, 0.f, nullptr);
+}
+
+void launch_advect_cfl1(const float4 *vel, const float *src, float *dst, Dims4 d, int nc,
+                        const float *maxn2, float cfl, int *flag, cudaStream_t s) {
+  BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
+  const int nb = grid_for(d.cells(), NT);
+  const float dt = (1.0f / (float)1) * 1.0f;
+  if (nc == 4)
+    k_advect<4><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt, maxn2, cfl, flag);
+  else
+    k_advect<1><<<nb, NT, 0, s>>>(vel, src, dst, d, bx, dt, maxn2, cfl, flag);
 }
 
 __global__ void k_deform_twoway(const float4 *__restrict__ vel,

@@ -138,8 +138,13 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
       } else {
         st->acc = (double)accuracy * residual;
         st->sigma = s;
-        if (s == 0.0 || s != s) st->done = CG_FAILED_SIGMA;
-        else st->done = CG_RUNNING;
+        if (s == 0.0 || s != s) {
+          st->retResidual = 1e10f;  // the caller's initial cgRes stays
+          st->done = CG_FAILED_SIGMA;
+        } else {
+          st->retResidual = 1.0f;   // residual / resIni before any iteration
+          st->done = CG_RUNNING;
+        }
       }
     }
   }

@@ -75,22 +75,38 @@ __device__ __forceinline__ void acc(float4 &v, const float4 &a) {
 __device__ __forceinline__ void acc(float &v, const float &a) { v += a; }
 
 // Issue the copies of the (x,y) slab at plane (zz, tt) into buffer `buf`.
+// Warp w copies slab rows w, w+4, ...; lane l copies columns l and l+32 of
+// each row, so the per-element work is one address add and one predicate.
 template <int S, int NC>
 __device__ __forceinline__ void issue_slab(typename VT<NC>::T *buf, const float *__restrict__ src,
                                            const Dims4 &d, int x0, int y0, int zz, int tt) {
   typedef SlabGeom<S> G;
   typedef typename VT<NC>::T T;
+  static_assert(G::W <= 64, "slab wider than two warps of columns");
   const bool plane_ok = zz >= 0 && zz < d.z && tt >= 0 && tt < d.t;
   const T *base = (const T *)src;
-  const idx_t plane = plane_ok ? ((idx_t)zz * d.sz() + (idx_t)tt * d.st()) : 0;
-  for (int e = threadIdx.x; e < G::W * G::H; e += NTHREADS) {
-    const int sy = e / G::W, sx = e - sy * G::W;
-    const int gx = x0 - S + sx, gy = y0 - S + sy;
-    const bool ok = plane_ok && gx >= 0 && gx < d.x && gy >= 0 && gy < d.y;
-    const T *g = ok ? base + plane + (idx_t)gy * d.x + gx : base;
-    T *s = buf + G::at(sy, sx);
-    if (NC == 4) cp_async16(s, g, ok ? 16 : 0);
-    else cp_async4(s, g, ok ? 4 : 0);
+  const T *plane = plane_ok ? base + ((idx_t)zz * d.sz() + (idx_t)tt * d.st()) : base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sx0 = lane, sx1 = lane + 32;
+  const int gx0 = x0 - S + sx0, gx1 = x0 - S + sx1;
+  const bool okx0 = gx0 >= 0 && gx0 < d.x;
+  const bool okx1 = sx1 < G::W && gx1 >= 0 && gx1 < d.x;
+  for (int sy = warp; sy < G::H; sy += NTHREADS / 32) {
+    const int gy = y0 - S + sy;
+    const bool oky = plane_ok && gy >= 0 && gy < d.y;
+    const T *row = plane + (idx_t)(oky ? gy : 0) * d.x;
+    {
+      const bool ok = oky && okx0;
+      T *s0 = buf + G::at(sy, sx0);
+      if (NC == 4) cp_async16(s0, ok ? row + gx0 : base, ok ? 16 : 0);
+      else cp_async4(s0, ok ? row + gx0 : base, ok ? 4 : 0);
+    }
+    if (sx1 < G::W) {
+      const bool ok = oky && okx1;
+      T *s1 = buf + G::at(sy, sx1);
+      if (NC == 4) cp_async16(s1, ok ? row + gx1 : base, ok ? 16 : 0);
+      else cp_async4(s1, ok ? row + gx1 : base, ok ? 4 : 0);
+    }
   }
 }
 

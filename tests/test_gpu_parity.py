@@ -229,6 +229,41 @@ def test_multiscale_flof_defaults(gpu, orc):
     assert err < pre and abs(err - werr) <= 0.05 * pre
 
 
+def test_multiscale_cfl_substeps(gpu, orc):
+    """cfl small enough that advections need several substeps: the device
+    check flags it and the call is redone with host-side substeps."""
+    dims = (24, 24, 24, 16)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    kw = dict(FLOF, doFinalProject=False, cfl=0.4, minGridSize=10)
+    want, werr, _ = orc.opticalFlowMultiscale4d(zv, i0, i1, **kw)
+    got, err, _ = _gpu_multiscale(i0, i1, **kw)
+    assert rel_l2(got, want) < REL_L2_DEFO
+    assert abs(err - werr) <= 1e-3 * abs(werr)
+
+
+def test_cfl_modes_agree_bitwise(gpu):
+    """The device-checked CFL substep count and the host-read one give the
+    same solve, bit for bit."""
+    from ofblend_gb300 import _lib
+    dims = (40, 36, 34, 20)
+    i0, i1 = drop_pair(dims)
+    kw = dict(FLOF, doFinalProject=True, cgAccuracy=1e-4, minGridSize=12)
+    out = []
+    for cfl_sync in (0, 1):
+        ctx = F.Context(0)
+        ctx.set_option(_lib.FLOF_OPT_CFL_SYNC, cfl_sync)
+        gv = F.Grid4Vec4(dims=dims, ctx=ctx)
+        g0 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(i0)
+        g1 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(i1)
+        err = F.opticalFlowMultiscale4d(gv, g0, g1, **kw)
+        out.append((gv.to_numpy(), err, F.last_solve_stats()["solves"]))
+        del gv, g0, g1
+        ctx.close()
+    for v, e, s in out[1:]:
+        assert np.array_equal(v, out[0][0]) and e == out[0][1] and s == out[0][2]
+
+
 def test_golden_multiscale_fixture(gpu):
     from conftest import ROOT
     import os
