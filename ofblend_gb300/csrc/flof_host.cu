@@ -101,12 +101,12 @@ struct Pool {
 enum KClass {
   KC_OTHER = 0, KC_ASSEMBLE, KC_MATVEC, KC_UPDATE, KC_DIRECTION, KC_COPYBACK, KC_BLUR,
   KC_PROJECT, KC_EXPOL, KC_ADVECT, KC_RESAMPLE, KC_LSDIFF, KC_REDUCE, KC_ELEMWISE, KC_BORDER,
-  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_COUNT
+  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_EXPOL_MASK, KC_COUNT
 };
 static const char *kc_names[KC_COUNT] = {
     "other", "of_assemble_init", "cg_matvec", "cg_update", "cg_direction", "of_copy_back",
     "gauss_blur", "project_cells", "expol_sweep", "advect", "resample", "ls_diff", "reduce",
-    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices"};
+    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices", "expol_mask"};
 
 struct ProfRec {
   int cls;
@@ -143,6 +143,7 @@ struct flof_ctx {
   // exceptions flagged in cfl_flag); 1: the host reads max |v| each time.
   int cfl_sync = 0;
   int *cfl_flag = nullptr;
+  int *dev_err = nullptr;  // device error word written by bounded waits
   int cfl_force_sync = 0;
   int profiling = 0;
   std::map<std::pair<uint32_t, int>, float *> wsum_cache;  // (sigma bits, radius)
@@ -274,6 +275,20 @@ int trunc_d(double v) {
   if (v >= 2147483647.0) return 2147483647;
   if (v <= -2147483648.0) return (-2147483647 - 1);
   return (int)v;
+}
+
+// Reads and clears the device error word (after the stream has drained).
+void check_device_errors(flof_ctx *c) {
+  CK(cudaMemcpyAsync(c->fres_h + 9, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  int e = 0;
+  memcpy(&e, c->fres_h + 9, sizeof(int));
+  if (e) {
+    CK(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    fail(FLOF_E_TIMEOUT, "a bounded wait on a TMA copy gave up (device error " +
+                             std::to_string(e) + ")");
+  }
 }
 
 void record_solve(flof_ctx *c, int sx, int iters, float res, int status) {
@@ -409,10 +424,19 @@ void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurTyp
     // original values): the state after the reference's two swaps.
     if (gauss_slab_supported(s, d)) {
       const float *ws = wsum_table(c, sigma, s, wtab);
-      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
-          launch_gauss_slab(a, tmp.f(), d, nc, s, wtab, ws, 1, c->stream));
-      KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
-          launch_gauss_slab(tmp.f(), a, d, nc, s, wtab, ws, 0, c->stream));
+      for (int pass = 0; pass < 2; ++pass) {
+        const float *src = pass == 0 ? a : tmp.f();
+        float *dst = pass == 0 ? tmp.f() : a;
+        const int zb = pass == 0 ? 1 : 0;
+        bool tma = false;
+        if (nc == 4)
+          KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+              tma = launch_gauss_tma((const float4 *)src, (float4 *)dst, d, s, wtab, ws, zb,
+                                     c->dev_err, c->stream));
+        if (!tma)
+          KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+              launch_gauss_slab(src, dst, d, nc, s, wtab, ws, zb, c->stream));
+      }
     } else {
       KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
           launch_gauss_pass(a, tmp.f(), d, nc, s, wtab, 1, c->stream));
@@ -529,6 +553,7 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
   if (!(postVelBlur < 1e30f) && postVelBlur == postVelBlur)
     fail(FLOF_E_ARG, "postVelBlur must be finite");
   DBuf marker(c, real_bytes(d)), tmp(c, vec_bytes(d));
+  DBuf mask(c, expol_mask_words(d) * sizeof(uint16_t));
   int singleStep = 0;
   if (postVelBlur < blurThreshold) singleStep = 1;
   float4 *A = dst;
@@ -540,8 +565,19 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
     KLP(c, KC_PROJECT, d.x, d.cells() * 44,
         launch_project_cells(dst, vel, phiOrg, phiTarget, marker.f(), d, threshPhi, maxIter,
                                c->stream));
+    if (doCvExtrapol > 0) {
+      // The sweeps only rewrite unmarked interior cells; both buffers carry
+      // the projected values everywhere else (the reference's tmp copy).
+      CK(cudaMemcpyAsync(B, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+      KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 4,
+          launch_expol_mask(marker.f(), (uint16_t *)mask.p, d, c->stream));
+    }
     for (int s = 0; s < doCvExtrapol; ++s) {
-      KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_slab(A, B, marker.f(), d, c->stream));
+      bool tma = false;
+      KLP(c, KC_EXPOL, d.x, d.cells() * 32,
+          tma = launch_expol_tma(A, B, (const uint16_t *)mask.p, d, c->dev_err, c->stream));
+      if (!tma)
+        KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_slab(A, B, marker.f(), d, c->stream));
       float4 *sw = A;
       A = B;
       B = sw;
@@ -836,6 +872,8 @@ FLOF_API int flof_ctx_create(int device, flof_ctx **out) {
       CK(cudaMalloc(&c->fpart, sizeof(float) * maxBlocks));
       CK(cudaMalloc(&c->cfl_flag, sizeof(int)));
       CK(cudaMemset(c->cfl_flag, 0, sizeof(int)));
+      CK(cudaMalloc(&c->dev_err, sizeof(int)));
+      CK(cudaMemset(c->dev_err, 0, sizeof(int)));
       CK(cudaMalloc(&c->counter, sizeof(unsigned int) * 8));
       CK(cudaMemset(c->counter, 0, sizeof(unsigned int) * 8));
       CK(cudaMalloc(&c->fres, sizeof(float) * 16));
@@ -867,6 +905,7 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   cudaFree(c->fpart);
   cudaFree(c->counter);
   cudaFree(c->cfl_flag);
+  cudaFree(c->dev_err);
   cudaFree(c->fres);
   cudaFree(c->dres);
   cudaFreeHost(c->fres_h);
@@ -1247,6 +1286,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
       throw;
     }
     c->stats = nullptr;
+    check_device_errors(c);
     local.err_final = e;
     local.syncs = c->syncs - syncs0;
     local.seconds =
@@ -1286,7 +1326,7 @@ FLOF_API int flof_opticalFlow4d(flof_ctx *c, flof_grid *vel, const flof_grid *i0
     DBuf vin(c, vel->bytes());
     CK(cudaMemcpyAsync(vin.p, vel->d, vel->bytes(), cudaMemcpyDeviceToDevice, c->stream));
     optical_flow_dim(c, vel->D(), vel->v(), vin.v(), i0->f(), i1->f(), a, iterations, residual);
-    CK(cudaStreamSynchronize(c->stream));
+    check_device_errors(c);
   });
 }
 
@@ -1313,7 +1353,7 @@ FLOF_API int flof_corrVelsOf4d(flof_ctx *c, flof_grid *dst, flof_grid *vel,
     set_ctx_device(c);
     corr_vels_of(c, vel->D(), dst->v(), vel->v(), phiOrg->f(), phiTarget->f(), threshPhi,
                  postVelBlur, resetBndWidth, maxIter, 1);
-    CK(cudaStreamSynchronize(c->stream));
+    check_device_errors(c);
   });
 }
 
@@ -1325,6 +1365,7 @@ FLOF_API int flof_gaussianBlur4d(flof_ctx *c, flof_grid *a, float sigma, int blu
     need(blurType == 1 || blurType == 2, "blurType must be 1 or 2");
     set_ctx_device(c);
     gauss_blur(c, a->f(), a->D(), a->nc(), sigma, blurType);
+    check_device_errors(c);
   });
 }
 

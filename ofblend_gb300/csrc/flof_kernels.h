@@ -155,6 +155,23 @@ void launch_gauss_slab(const float *src, float *dst, Dims4 d, int nc, int s,
 void launch_expol_slab(const float4 *in, float4 *out, const float *mark, Dims4 d,
                        cudaStream_t st);
 
+// TMA-staged versions (flof_tma.cu) for Vec4 grids: same results bit for
+// bit.  They return false when no tensor map can be built (the caller then
+// uses the cp.async kernels).  A block whose bounded mbarrier wait runs out
+// stores FLOF_DEV_ERR_TMA_TIMEOUT in *err and returns.
+constexpr int FLOF_DEV_ERR_TMA_TIMEOUT = 1;
+bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const float *wtab,
+                      const float *wsum_dev, int zero_border, int *err, cudaStream_t st);
+// The TMA extrapolation sweep writes only the cells it updates (unmarked
+// interior cells), so its output buffer must already hold the input's values
+// at every other cell (a copy of the input made once per projection round).
+// Which cells those are comes from a packed mask that launch_expol_mask
+// builds from the marker once per round: expol_mask_words(d) 16-bit words.
+size_t expol_mask_words(Dims4 d);
+void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st);
+bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                      cudaStream_t st);
+
 // ---- projection correction ------------------------------------------------------
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,

@@ -1,0 +1,376 @@
+// flof_tma.cu -- TMA-staged slab kernels for the dense 4D stencils on Vec4
+// grids: the Gaussian velocity blur (knGaussianBlur, optflow4d.cpp:132-158,
+// radius 1 and 2) and the extrapolation sweep (knCvExpolBlur4d, :613-626).
+//
+// Same arithmetic as flof_stencil.cu: every output sums its (2S+1)^4
+// neighbourhood in the reference's order (t, z, y, x) with float adds in
+// sequence.  A block owns a 32-column (x,y) tile at one z for DT consecutive t
+// planes and walks the input slabs those planes need once, in (t, z) order;
+// each (x,y) slab with its S-cell halo is brought into shared memory by one
+// cp.async.bulk.tensor copy issued by a single thread, completion signalled
+// on an mbarrier, with NSTAGE slabs in flight.  For the extrapolation sweep
+// four output planes share every slab, which halves the L2-to-SM traffic
+// that bounds it.  The
+// tensor map views the float4 grid as a 5D float tensor (component, x, y, z,
+// t), so the innermost coordinate is always 0 (16-byte aligned) and cells
+// outside the grid arrive as zeros, which leave a running float sum
+// unchanged.  Lane l of a warp computes column x0+l for RY consecutive rows of
+// each plane, so each 8-lane shared-memory phase reads 128 contiguous bytes
+// of the dense TMA layout.
+//
+// Every wait on an mbarrier is bounded; a block that gives up records
+// FLOF_DEV_ERR_TMA_TIMEOUT in the context's device error word, waits (again
+// bounded) for its copies in flight and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "flof_kernels.h"
+
+namespace flof {
+
+namespace {
+
+constexpr int TX = 32;                // tile width: one column per lane
+constexpr int NWARP = 4;
+constexpr int NTHR = TX * NWARP;      // 128
+constexpr int WAIT_LIMIT = 1 << 22;   // try_wait polls before giving up
+
+// Tile geometry: RY rows per thread, DT consecutive t planes per block,
+// NSTAGE slab buffers in flight.
+template <int S, int RY_, int DT_, int NSTAGE_>
+struct TG {
+  static constexpr int RY = RY_, DT = DT_, NSTAGE = NSTAGE_;
+  static constexpr int TY = NWARP * RY;
+  static constexpr int W = TX + 2 * S, H = TY + 2 * S, N = W * H;
+  static constexpr int BYTES = N * 16;                   // one slab
+  static constexpr int STRIDE = (BYTES + 127) / 128 * 128;  // slab start spacing
+  static constexpr int SMEM = NSTAGE * STRIDE;
+};
+// The blur (S = 1, 2) is bound by its multiply-adds: one t plane, 32 rows.
+// The extrapolation sweep has one add per tap and is bound by how fast slabs
+// reach shared memory: four t planes share every slab, four slabs in flight.
+template <int S> using BlurGeom = TG<S, 8, 1, 2>;
+using ExpolGeom = TG<1, 4, 4, 4>;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  for (int i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map, int x, int y,
+                                              int z, int t, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(0), "r"(x), "r"(y), "r"(z), "r"(t), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void mac4(float4 &v, float w, const float4 &a) {
+  v.x += w * a.x;
+  v.y += w * a.y;
+  v.z += w * a.z;
+  v.w += w * a.w;
+}
+__device__ __forceinline__ void acc4(float4 &v, const float4 &a) {
+  v.x += a.x;
+  v.y += a.y;
+  v.z += a.z;
+  v.w += a.w;
+}
+
+template <int S>
+__device__ __forceinline__ int clip_code_t(int c, int ext) {
+  int lo = S - c;
+  lo = lo < 0 ? 0 : lo;
+  int hi = c + S - (ext - 1);
+  hi = hi < 0 ? 0 : hi;
+  return lo * (S + 1) + hi;
+}
+
+}  // namespace
+
+struct WTabT {
+  float w[40];
+};
+
+// MODE 0: Gaussian blur pass; MODE 1: extrapolation sweep.  A block computes
+// the outputs of DT consecutive t planes at one z.  It walks the input slabs
+// (tt, zz) of the union of their neighbourhoods in lexicographic order; for a
+// fixed output plane t_o that order is the reference's (vt, zk) order with
+// vt = tt - t_o, zk = zz - z, so every output still adds its taps in the
+// reference's sequence while each slab is fetched once for all DT planes.
+template <int S, int MODE, class G>
+__global__ void __launch_bounds__(NTHR)
+k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
+           int tiles_x, const float *__restrict__ wsum, const uint16_t *__restrict__ fixed,
+           WTabT wt, int zero_border, int *err) {
+  constexpr int RY = G::RY, DT = G::DT, NS = G::NSTAGE;
+  extern __shared__ __align__(128) unsigned char raw[];
+  __shared__ __align__(8) uint64_t bar[NS];
+  __shared__ float wsh[40];
+
+  const int tile = blockIdx.x;
+  const int x0 = (tile % tiles_x) * TX, y0 = (tile / tiles_x) * G::TY;
+  const int z = blockIdx.y, t0 = blockIdx.z * DT;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x = x0 + tx;
+  const int ygroups = (d.y + RY - 1) / RY;
+  const int yg = y0 / RY + ty;
+  // MODE 1: bit o*RY+q set = cell (x, y0+RY*ty+q, z, t0+o) keeps its value
+  // (loaded now, used after the slab walk)
+  unsigned keep = 0xffffu;
+  if (MODE == 1 && x < d.x && yg < ygroups)
+    keep = __ldg(fixed + (((size_t)blockIdx.z * d.z + z) * ygroups + yg) * d.x + x);
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int b = 0; b < NS; ++b) mbar_init(&bar[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (MODE == 0 && threadIdx.x < 40) wsh[threadIdx.x] = wt.w[threadIdx.x];
+  __syncthreads();
+
+  constexpr int K = 2 * S + 1;
+  constexpr int NP = (DT + 2 * S) * K;  // slabs (tt, zz), tt-major
+  // slab p lives in buffer p % NS; its barrier completes phase (p / NS) & 1
+  auto issue = [&](int p) {
+    uint64_t *b = &bar[p % NS];
+    mbar_expect_tx(b, G::BYTES);
+    tma_load_slab(raw + (p % NS) * G::STRIDE, &map, x0 - S, y0 - S, z + (p % K - S),
+                  t0 - S + p / K, b);
+  };
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int p = 0; p < NS - 1; ++p)
+      if (p < NP) issue(p);
+  }
+
+  float4 val[DT][RY];
+#pragma unroll
+  for (int o = 0; o < DT; ++o)
+#pragma unroll
+    for (int q = 0; q < RY; ++q) val[o][q] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (int p = 0; p < NP; ++p) {
+    const int tt = t0 - S + p / K, zk = p % K - S;
+    // buffer (p - 1) % NS was released by the barrier that ended step p - 1
+    if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
+    const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
+        // let the copies in flight land before the block's shared memory goes
+        for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
+      }
+      __syncthreads();
+      return;
+    }
+    const float4 *cur = (const float4 *)(raw + (p % NS) * G::STRIDE);
+    // slab rows RY*ty .. RY*ty+RY-1+2S feed output rows RY*ty+q via yj = k-q-S
+#pragma unroll
+    for (int k = 0; k < RY + 2 * S; ++k) {
+      const float4 *row = cur + (RY * ty + k) * G::W + tx;
+      float4 a[2 * S + 1];
+#pragma unroll
+      for (int m = 0; m <= 2 * S; ++m) a[m] = row[m];
+#pragma unroll
+      for (int o = 0; o < DT; ++o) {
+        const int vt = tt - (t0 + o);
+        if (vt < -S || vt > S) continue;
+#pragma unroll
+        for (int q = 0; q < RY; ++q) {
+          const int yj = k - q - S;
+          if (yj < -S || yj > S) continue;
+          if (MODE == 0) {
+            const int base = vt * vt + zk * zk + yj * yj;
+            float wx[S + 1];
+#pragma unroll
+            for (int e = 0; e <= S; ++e) wx[e] = wsh[base + e * e];
+#pragma unroll
+            for (int xi = -S; xi <= S; ++xi) mac4(val[o][q], wx[xi < 0 ? -xi : xi], a[xi + S]);
+          } else {
+#pragma unroll
+            for (int xi = -S; xi <= S; ++xi) acc4(val[o][q], a[xi + S]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  if (x >= d.x) return;
+  constexpr int P1 = (S + 1) * (S + 1);
+#pragma unroll
+  for (int o = 0; o < DT; ++o) {
+    const int t = t0 + o;
+    if (t >= d.t) break;
+    const bool zt_inner = z >= 1 && z < d.z - 1 && t >= 1 && t < d.t - 1;
+    const int code_zt =
+        MODE == 0 ? ((clip_code_t<S>(t, d.t) * P1 + clip_code_t<S>(z, d.z)) * P1) : 0;
+#pragma unroll
+    for (int q = 0; q < RY; ++q) {
+      const int y = y0 + RY * ty + q;
+      if (y >= d.y) continue;
+      const idx_t id = d.index(x, y, z, t);
+      const float4 v = val[o][q];
+      if (MODE == 0) {
+        if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
+          if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+          continue;
+        }
+        const float ws =
+            __ldg(wsum + (code_zt + clip_code_t<S>(y, d.y)) * P1 + clip_code_t<S>(x, d.x));
+        dst[id] = make_float4(v.x / ws, v.y / ws, v.z / ws, v.w / ws);
+      } else {
+        if (keep >> (o * RY + q) & 1u) continue;
+        dst[id] = make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
+      }
+    }
+  }
+}
+
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor map of a float4 grid as a 5D float tensor (4, X, Y, Z, T) with a
+// (4, W, H, 1, 1) box.
+bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn || ((uintptr_t)base & 15)) return false;
+  const cuuint64_t dims[5] = {4, (cuuint64_t)d.x, (cuuint64_t)d.y, (cuuint64_t)d.z,
+                              (cuuint64_t)d.t};
+  const cuuint64_t strides[4] = {16, (cuuint64_t)16 * d.x, (cuuint64_t)16 * d.x * d.y,
+                                 (cuuint64_t)16 * d.x * d.y * d.z};
+  const cuuint32_t box[5] = {4, (cuuint32_t)W, (cuuint32_t)H, 1, 1};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, (void *)base, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int S, int MODE, class G>
+bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
+                const uint16_t *fixed, const float *w, int zero_border, int *err,
+                cudaStream_t st) {
+  const int tgroups = (d.t + G::DT - 1) / G::DT;
+  if (d.z > 65535 || tgroups > 65535) return false;
+  CUtensorMap map;
+  if (!encode_slab_map(&map, src, d, G::W, G::H)) return false;
+  const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + G::TY - 1) / G::TY;
+  dim3 grid(tiles_x * tiles_y, d.z, tgroups);
+  const size_t smem = G::SMEM;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_slab_tma<S, MODE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    attr = true;
+  }
+  WTabT wt;
+  for (int i = 0; i < 40; ++i) wt.w[i] = (w && i <= 4 * S * S) ? w[i] : 0.f;
+  k_slab_tma<S, MODE, G><<<grid, NTHR, smem, st>>>(map, dst, d, tiles_x, wsum, fixed, wt,
+                                                  zero_border, err);
+  return true;
+}
+
+}  // namespace
+
+bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const float *wtab,
+                      const float *wsum_dev, int zero_border, int *err, cudaStream_t st) {
+  if (s == 1)
+    return launch_tma<1, 0, BlurGeom<1>>(src, dst, d, wsum_dev, nullptr, wtab, zero_border, err,
+                                         st);
+  if (s == 2)
+    return launch_tma<2, 0, BlurGeom<2>>(src, dst, d, wsum_dev, nullptr, wtab, zero_border, err,
+                                         st);
+  return false;
+}
+
+namespace {
+
+// One 16-bit word per sweep thread: (x, y group of RY rows, z, t group of DT
+// planes), x fastest.  A bit is set for each cell of the thread's RY x DT
+// outputs that the sweep leaves alone: marked, outside the interior
+// (knCvExpolBlur4d runs over bnd = 1), or past the grid's end.
+__global__ void k_expol_mask(const float *__restrict__ mark, uint16_t *__restrict__ mask,
+                             Dims4 d, int ygroups, long long nwords) {
+  constexpr int RY = ExpolGeom::RY, DT = ExpolGeom::DT;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nwords;
+       w += (long long)gridDim.x * blockDim.x) {
+    const int x = (int)(w % d.x);
+    long long r = w / d.x;
+    const int yg = (int)(r % ygroups);
+    r /= ygroups;
+    const int z = (int)(r % d.z);
+    const int tg = (int)(r / d.z);
+    unsigned bits = 0;
+    for (int o = 0; o < DT; ++o)
+      for (int q = 0; q < RY; ++q) {
+        const int y = yg * RY + q, t = tg * DT + o;
+        const bool inner = x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1 && z >= 1 &&
+                           z < d.z - 1 && t >= 1 && t < d.t - 1;
+        if (!inner || __ldg(mark + d.index(x, y, z, t)) != 0.f) bits |= 1u << (o * RY + q);
+      }
+    mask[w] = (uint16_t)bits;
+  }
+}
+
+}  // namespace
+
+size_t expol_mask_words(Dims4 d) {
+  return (size_t)d.x * ((d.y + ExpolGeom::RY - 1) / ExpolGeom::RY) * d.z *
+         ((d.t + ExpolGeom::DT - 1) / ExpolGeom::DT);
+}
+
+void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st) {
+  const long long n = (long long)expol_mask_words(d);
+  const int ygroups = (d.y + ExpolGeom::RY - 1) / ExpolGeom::RY;
+  k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, mask, d, ygroups, n);
+}
+
+bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                      cudaStream_t st) {
+  return launch_tma<1, 1, ExpolGeom>(in, out, d, nullptr, mask, nullptr, 0, err, st);
+}
+
+}  // namespace flof

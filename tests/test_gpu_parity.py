@@ -172,8 +172,9 @@ def test_opticalflow4d_single_level(gpu, orc, blur):
     assert rel_l2(gv.to_numpy(), want) < REL_L2_DEFO
 
 
-def test_corrvelsof_bitexact(gpu, orc):
-    dims = (20, 20, 20, 16)
+# the second size leaves partial tiles in x, y and t in the staged kernels
+@pytest.mark.parametrize("dims", [(20, 20, 20, 16), (37, 21, 19, 15)])
+def test_corrvelsof_bitexact(gpu, orc, dims):
     i0, i1 = drop_pair(dims)
     r = np.random.default_rng(19)
     vel = (r.standard_normal(i0.shape + (4,)) * 0.8).astype(np.float32)
