@@ -216,8 +216,15 @@ class Workload:
 
 
 def roofline(records, R, peak, peak_kind, traffic):
-    per = {}
+    """Roofline of the kernel class with the most device time at the full
+    grid size R, and the device time of every class over all sizes (the
+    pyramid levels and the hi-res frames included)."""
+    per, every = {}, {}
     for name, sx, nb, ms in records:
+        e = every.setdefault(name, [0, 0.0, 0.0])
+        e[0] += 1
+        e[1] += nb
+        e[2] += ms
         if sx != R:
             continue
         e = per.setdefault(name, [0, 0.0, 0.0])
@@ -235,7 +242,8 @@ def roofline(records, R, peak, peak_kind, traffic):
           "launches": n, "bytes_per_launch": nb / n, "ms_per_launch": ms / n,
           "peak_source": f"hbm_gbs of {peak_kind}"}
     share = {k: {"launches": v[0], "ms": round(v[2], 3),
-                 "GBps": round(v[1] / (v[2] * 1e-3) / 1e9, 1) if v[2] > 0 else None} for k, v in per.items()}
+                 "GBps": round(v[1] / (v[2] * 1e-3) / 1e9, 1) if v[2] > 0 else None}
+             for k, v in sorted(every.items(), key=lambda kv: -kv[1][2])}
     return rl, share
 
 
@@ -362,6 +370,7 @@ def run_gpu(a):
         "gpu_launches": launches,
         "clocks": clk,
         "kernel_share": share,
+        "kernel_ms_per_step": round(sum(r[3] for r in recs) / a.steps, 3),
         "cg_iterations_level0": [[x[1] for x in s if x[0] == a.res] for s in iters[:2]],
     }
     if rank == 0 and not a.no_cpu_baseline:

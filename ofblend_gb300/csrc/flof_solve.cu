@@ -166,59 +166,121 @@ void launch_of_assemble_init(const float *i0w, const float *i1,
 
 // q = A p over the interior rows; applyMat order: 8 neighbour terms
 // (-t,-z,-y,-x,+x,+y,+z,+t) then the 4 block terms.
-__global__ void __launch_bounds__(NT)
+//
+// A thread owns one interior (x,y) column cell at one z and walks MV_TT
+// consecutive t planes, keeping p at t-1, t and t+1 in registers, so the -t
+// and +t terms cost no extra load, and loading the next plane's operands
+// while it computes the current one.  A work item is (run of MV_NT cells of
+// the interior (x,y) plane, z, t chunk) with the (x,y) run fastest, so the
+// blocks resident at one time cover neighbouring z at the same t chunk and
+// the z-neighbour loads hit L2.  The grid is persistent (a fixed number of
+// blocks per SM); p.Ap is accumulated per thread in float-float and summed
+// in double by the last block to finish, in a fixed order.
+constexpr int MV_NT = 128;
+constexpr int MV_TT = 8;
+
+struct MVShape {
+  FastDiv fx;        // interior x extent
+  int nxy;           // interior (x,y) cells
+  int runs;          // ceil(nxy / MV_NT)
+  FastDiv fruns, fz;  // runs, interior z extent
+  int items;         // runs * (Z-2) * tchunks
+};
+
+__device__ __forceinline__ void mv_acc(float4 &v, float o, const float4 a) {
+  v.x += o * a.x;
+  v.y += o * a.y;
+  v.z += o * a.z;
+  v.w += o * a.w;
+}
+
+// The operands of one cell other than p at t-1 and t.
+struct MVLoads {
+  float4 pp, gg, zm, ym, xm, xp, yp, zp;
+};
+__device__ __forceinline__ void mv_load(MVLoads &a, const float4 *__restrict__ p,
+                                        const float4 *__restrict__ g, idx_t id, idx_t sY,
+                                        idx_t sZ, idx_t sT) {
+  a.pp = __ldg(p + id + sT);
+  a.gg = __ldg(g + id);
+  a.zm = __ldg(p + id - sZ);
+  a.ym = __ldg(p + id - sY);
+  a.xm = __ldg(p + id - 1);
+  a.xp = __ldg(p + id + 1);
+  a.yp = __ldg(p + id + sY);
+  a.zp = __ldg(p + id + sZ);
+}
+
+// OFFD: the neighbour terms are present (applyMat skips them for a zero
+// off-diagonal, optflow4d.cpp:215).
+template <bool OFFD>
+__global__ void __launch_bounds__(MV_NT)
 k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
-            float4 *__restrict__ q, Dims4 d, BoxDecoder bx, uint32_t nint,
-            OFConsts c, CGState *st, double *dpart) {
+            float4 *__restrict__ q, Dims4 d, MVShape sh, OFConsts c, CGState *st,
+            double *dpart) {
   if (st->done) return;
-  __shared__ double shd[NT / 32];
+  __shared__ double shd[MV_NT / 32];
   FF dot = {0.f, 0.f};
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   const float o = c.offd;
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
-       n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    const float4 pc = __ldg(p + id);
-    const float4 gg = __ldg(g + id);
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (o != 0.f) {
-      const idx_t off[8] = {-sT, -sZ, -sY, -1, 1, sY, sZ, sT};
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const float4 pn = __ldg(p + id + off[m]);
-        v.x += o * pn.x;
-        v.y += o * pn.y;
-        v.z += o * pn.z;
-        v.w += o * pn.w;
+  for (int item = blockIdx.x; item < sh.items; item += gridDim.x) {
+    const uint32_t r1 = sh.fruns.div((uint32_t)item);
+    const int run = item - (int)r1 * sh.runs;
+    const uint32_t tc = sh.fz.div(r1);
+    const int k = 1 + (int)(r1 - tc * sh.fz.d);
+    const int n = run * MV_NT + threadIdx.x;
+    if (n >= sh.nxy) continue;
+    const uint32_t jj = sh.fx.div((uint32_t)n);
+    const int i = 1 + (n - (int)(jj * sh.fx.d)), j = 1 + (int)jj;
+    const int l0 = 1 + (int)tc * MV_TT;
+    const int l1 = min(l0 + MV_TT, d.t - 1);
+    idx_t id = d.index(i, j, k, l0);
+    float4 pm = __ldg(p + id - sT), pc = __ldg(p + id);
+    MVLoads cur, nxt;
+    mv_load(cur, p, g, id, sY, sZ, sT);
+    for (int l = l0; l < l1; ++l, id += sT) {
+      // the last plane reloads its own operands instead of reading past l1
+      mv_load(nxt, p, g, l + 1 < l1 ? id + sT : id, sY, sZ, sT);
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (OFFD) {
+        mv_acc(v, o, pm);
+        mv_acc(v, o, cur.zm);
+        mv_acc(v, o, cur.ym);
+        mv_acc(v, o, cur.xm);
+        mv_acc(v, o, cur.xp);
+        mv_acc(v, o, cur.yp);
+        mv_acc(v, o, cur.zp);
+        mv_acc(v, o, cur.pp);
       }
-    }
-    const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
-    const float pv[4] = {pc.x, pc.y, pc.z, pc.w};
-    float vv[4] = {v.x, v.y, v.z, v.w};
+      const float gv[4] = {cur.gg.x, cur.gg.y, cur.gg.z, cur.gg.w};
+      const float pv[4] = {pc.x, pc.y, pc.z, pc.w};
+      float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-    for (int dd = 0; dd < 4; ++dd) {
+      for (int dd = 0; dd < 4; ++dd) {
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        float b = gv[dd] * gv[m];
-        if (dd == m) b = b + c.diag;
-        vv[dd] += b * pv[m];
+        for (int m = 0; m < 4; ++m) {
+          float b = gv[dd] * gv[m];
+          if (dd == m) b = b + c.diag;
+          vv[dd] += b * pv[m];
+        }
       }
+      const float4 qq = make_float4(vv[0], vv[1], vv[2], vv[3]);
+      q[id] = qq;
+      ff_add(dot, pc.x * qq.x);
+      ff_add(dot, pc.y * qq.y);
+      ff_add(dot, pc.z * qq.z);
+      ff_add(dot, pc.w * qq.w);
+      pm = pc;
+      pc = cur.pp;
+      cur = nxt;
     }
-    const float4 qq = make_float4(vv[0], vv[1], vv[2], vv[3]);
-    q[id] = qq;
-    ff_add(dot, pc.x * qq.x);
-    ff_add(dot, pc.y * qq.y);
-    ff_add(dot, pc.z * qq.z);
-    ff_add(dot, pc.w * qq.w);
   }
-  const double bd = block_sum<NT>(ff_value(dot), shd);
+  const double bd = block_sum<MV_NT>(ff_value(dot), shd);
   if (threadIdx.x == 0) dpart[blockIdx.x] = bd;
   if (last_block_arrives(&st->counter[1])) {
     double s = 0.0;
     for (int q2 = threadIdx.x; q2 < (int)gridDim.x; q2 += blockDim.x) s += __ldcg(dpart + q2);
-    s = block_sum<NT>(s, shd);
+    s = block_sum<MV_NT>(s, shd);
     if (threadIdx.x == 0) {
       st->pAp = s;
       st->alpha = st->sigma / s;
@@ -229,8 +291,30 @@ k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
 
 void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
                       OFConsts c, CGState *st, double *dpart, cudaStream_t s) {
-  k_cg_matvec<<<cg_blocks(d), NT, 0, s>>>(p, g, q, d, interior_decoder(d),
-                                          interior_count(d), c, st, dpart);
+  MVShape sh;
+  const int ex = d.x > 2 ? d.x - 2 : 1, ey = d.y > 2 ? d.y - 2 : 1;
+  const int ez = d.z > 2 ? d.z - 2 : 1;
+  const int tchunks = d.t > 2 ? (d.t - 2 + MV_TT - 1) / MV_TT : 0;
+  const bool empty = d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3;
+  sh.fx = FastDiv((uint32_t)ex);
+  sh.nxy = empty ? 0 : ex * ey;
+  sh.runs = (ex * ey + MV_NT - 1) / MV_NT;
+  sh.fruns = FastDiv((uint32_t)sh.runs);
+  sh.fz = FastDiv((uint32_t)ez);
+  sh.items = empty ? 0 : sh.runs * ez * tchunks;
+  const bool offd = c.offd != 0.f;
+  static int per_sm[2] = {0, 0};
+  if (!per_sm[offd]) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm[offd], offd ? k_cg_matvec<true> : k_cg_matvec<false>, MV_NT, 0);
+    if (per_sm[offd] < 1) per_sm[offd] = 1;
+  }
+  int blocks = sm_count() * per_sm[offd];
+  if (blocks > sh.items) blocks = sh.items > 0 ? sh.items : 1;
+  if (offd)
+    k_cg_matvec<true><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+  else
+    k_cg_matvec<false><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
 }
 
 // x += alpha p; r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).

@@ -158,14 +158,15 @@ def test_calc_ls_diff(gpu, orc):
 # ---------------------------------------------------------------------------
 # solve
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("blur", [0.0, 4.0])
-def test_opticalflow4d_single_level(gpu, orc, blur):
+# wSmooth 0 gives a zero off-diagonal, for which applyMat skips the neighbour terms
+@pytest.mark.parametrize("blur,ws", [(0.0, 0.001), (4.0, 0.001), (0.0, 0.0)])
+def test_opticalflow4d_single_level(gpu, orc, blur, ws):
     dims = (24, 24, 24, 20)
     i0, i1 = drop_pair(dims)
     zv = np.zeros(i0.shape + (4,), np.float32)
-    want, wit, wres = orc.opticalFlow4d(zv, i0, i1, 0.001, 0.0001, blur, 1e-4, 0.1)
+    want, wit, wres = orc.opticalFlow4d(zv, i0, i1, ws, 0.0001, blur, 1e-4, 0.1)
     gv = grid_of(zv)
-    it, res = F.opticalFlow4d(gv, grid_of(i0), grid_of(i1), wSmooth=0.001, wEnergy=0.0001,
+    it, res = F.opticalFlow4d(gv, grid_of(i0), grid_of(i1), wSmooth=ws, wEnergy=0.0001,
                               postVelBlur=blur, cgAccuracy=1e-4, resetBndWidth=0.1)
     assert abs(it - wit) <= 2
     assert res <= 1e-4
