@@ -20,289 +20,12 @@
 #include <unordered_map>
 #include <vector>
 
-#include "../../include/flof_gb300.h"
-#include "flof_kernels.h"
+#include "flof_internal.h"
 
 using namespace flof;
+using namespace fh;
 
 namespace {
-
-thread_local std::string g_last_error;
-
-struct FlofError {
-  int code;
-  std::string msg;
-};
-
-[[noreturn]] void fail(int code, const std::string &msg) { throw FlofError{code, msg}; }
-
-void cuda_check(cudaError_t e, const char *what) {
-  if (e == cudaSuccess) return;
-  const int code = (e == cudaErrorMemoryAllocation) ? FLOF_E_OOM : FLOF_E_CUDA;
-  fail(code, std::string(what) + ": " + cudaGetErrorString(e));
-}
-#define CK(call) cuda_check((call), #call)
-
-struct Pool {
-  std::unordered_map<size_t, std::vector<void *>> free_list;
-  std::unordered_map<void *, size_t> owned;
-  size_t bytes = 0;
-
-  void *get(size_t n) {
-    if (n == 0) n = 16;
-    n = (n + 255) & ~size_t(255);
-    auto it = free_list.find(n);
-    if (it != free_list.end() && !it->second.empty()) {
-      void *p = it->second.back();
-      it->second.pop_back();
-      return p;
-    }
-    void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      trim();
-      e = cudaMalloc(&p, n);
-      if (e != cudaSuccess) {
-        cudaGetLastError();
-        fail(FLOF_E_OOM, "device allocation of " + std::to_string(n) + " bytes failed");
-      }
-    }
-    owned[p] = n;
-    bytes += n;
-    return p;
-  }
-  void put(void *p) {
-    if (!p) return;
-    auto it = owned.find(p);
-    if (it == owned.end()) return;
-    free_list[it->second].push_back(p);
-  }
-  void trim() {
-    for (auto &kv : free_list) {
-      for (void *p : kv.second) {
-        cudaFree(p);
-        owned.erase(p);
-        bytes -= kv.first;
-      }
-      kv.second.clear();
-    }
-  }
-  void release_all() {
-    for (auto &kv : owned) cudaFree(kv.first);
-    owned.clear();
-    free_list.clear();
-    bytes = 0;
-  }
-};
-
-}  // namespace
-
-enum KClass {
-  KC_OTHER = 0, KC_ASSEMBLE, KC_MATVEC, KC_UPDATE, KC_DIRECTION, KC_COPYBACK, KC_BLUR,
-  KC_PROJECT, KC_EXPOL, KC_ADVECT, KC_RESAMPLE, KC_LSDIFF, KC_REDUCE, KC_ELEMWISE, KC_BORDER,
-  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_EXPOL_MASK, KC_COUNT
-};
-static const char *kc_names[KC_COUNT] = {
-    "other", "of_assemble_init", "cg_matvec", "cg_update", "cg_direction", "of_copy_back",
-    "gauss_blur", "project_cells", "expol_sweep", "advect", "resample", "ls_diff", "reduce",
-    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices", "expol_mask"};
-
-struct ProfRec {
-  int cls;
-  int size_x;
-  double bytes;
-  cudaEvent_t e0, e1;
-};
-
-struct LatsData {
-  const flof_grid *defo = nullptr;
-  void *vt = nullptr;  // blended t-slice (Vec4, X*Y*Z of the defo)
-  int lastT = -1;
-};
-
-struct flof_ctx {
-  int device = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  Pool pool;
-  CGState *st = nullptr;    // device
-  CGState *st_h = nullptr;  // pinned host mirror
-  double *dpart = nullptr;
-  float *fpart = nullptr;
-  unsigned int *counter = nullptr;  // 8 zeroed counters
-  float *fres = nullptr;            // 16 device scalars
-  double *dres = nullptr;
-  float *fres_h = nullptr;          // pinned
-  double *dres_h = nullptr;
-  long long launches = 0;
-  int syncs = 0;
-  std::map<int, LatsData> lats;
-  flof_solve_stats *stats = nullptr;
-  // 0: CFL substep counts are checked on the device (one substep assumed,
-  // exceptions flagged in cfl_flag); 1: the host reads max |v| each time.
-  int cfl_sync = 0;
-  int *cfl_flag = nullptr;
-  int *dev_err = nullptr;  // device error word written by bounded waits
-  int cfl_force_sync = 0;
-  int profiling = 0;
-  std::map<std::pair<uint32_t, int>, float *> wsum_cache;  // (sigma bits, radius)
-  std::vector<ProfRec> recs;
-  std::vector<cudaEvent_t> ev_pool;
-  size_t ev_used = 0;
-};
-
-struct flof_grid {
-  flof_ctx *ctx = nullptr;
-  int dims[4] = {0, 0, 0, 0};
-  int elem = FLOF_REAL;
-  void *d = nullptr;
-  bool owned = false;
-  // OptInit pins the deformation grid it reads from; destroying a pinned
-  // grid is deferred until the last Finish releases it.
-  int pins = 0;
-  bool destroy_pending = false;
-  Dims4 D() const { return Dims4{dims[0], dims[1], dims[2], dims[3]}; }
-  int nc() const { return elem == FLOF_VEC4 ? 4 : 1; }
-  long long cells() const { return (long long)dims[0] * dims[1] * dims[2] * dims[3]; }
-  size_t bytes() const { return (size_t)cells() * nc() * sizeof(float); }
-  float *f() const { return (float *)d; }
-  float4 *v() const { return (float4 *)d; }
-};
-
-static void grid_free(flof_grid *g) {
-  if (g->owned && g->d) {
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
-    cudaFree(g->d);
-  }
-  delete g;
-}
-
-static void grid_unpin(flof_grid *g) {
-  if (!g) return;
-  if (g->pins > 0) g->pins--;
-  if (g->pins == 0 && g->destroy_pending) grid_free(g);
-}
-
-namespace {
-
-// RAII device buffer from the context pool.
-struct DBuf {
-  flof_ctx *c = nullptr;
-  void *p = nullptr;
-  DBuf() {}
-  DBuf(flof_ctx *ctx, size_t n) : c(ctx), p(ctx->pool.get(n)) {}
-  DBuf(const DBuf &) = delete;
-  DBuf &operator=(const DBuf &) = delete;
-  DBuf(DBuf &&o) noexcept : c(o.c), p(o.p) { o.p = nullptr; }
-  DBuf &operator=(DBuf &&o) noexcept {
-    if (this != &o) {
-      release();
-      c = o.c;
-      p = o.p;
-      o.p = nullptr;
-    }
-    return *this;
-  }
-  ~DBuf() { release(); }
-  void release() {
-    if (p && c) c->pool.put(p);
-    p = nullptr;
-  }
-  float *f() const { return (float *)p; }
-  float4 *v() const { return (float4 *)p; }
-};
-
-inline size_t real_bytes(Dims4 d) { return (size_t)d.cells() * sizeof(float); }
-inline size_t vec_bytes(Dims4 d) { return (size_t)d.cells() * sizeof(float4); }
-
-// Kernel launch with optional event tracing: when the context profiles,
-// every launch is bracketed by two CUDA events on the context stream and
-// recorded with its kernel class, the X extent of its grid and its
-// algorithmic bytes (compulsory reads + writes).
-#define KLP(ctx, cls, sx, nbytes, call)                                   \
-  do {                                                                     \
-    flof_ctx *_c = (ctx);                                                  \
-    cudaEvent_t _e0 = nullptr, _e1 = nullptr;                              \
-    if (_c->profiling) {                                                   \
-      _e0 = prof_event(_c);                                                \
-      _e1 = prof_event(_c);                                                \
-      CK(cudaEventRecord(_e0, _c->stream));                                \
-    }                                                                      \
-    call;                                                                  \
-    ++_c->launches;                                                        \
-    if (_c->profiling) {                                                   \
-      CK(cudaEventRecord(_e1, _c->stream));                                \
-      _c->recs.push_back(ProfRec{(cls), (sx), (double)(nbytes), _e0, _e1}); \
-    }                                                                      \
-  } while (0)
-#define KL(ctx, call) KLP(ctx, KC_OTHER, 0, 0, call)
-
-inline long long nint(Dims4 d) {
-  if (d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3) return 0;
-  return (long long)(d.x - 2) * (d.y - 2) * (d.z - 2) * (d.t - 2);
-}
-
-cudaEvent_t prof_event(flof_ctx *c) {
-  if (c->ev_used == c->ev_pool.size()) {
-    cudaEvent_t e;
-    CK(cudaEventCreate(&e));
-    c->ev_pool.push_back(e);
-  }
-  return c->ev_pool[c->ev_used++];
-}
-
-void sync(flof_ctx *c) {
-  CK(cudaStreamSynchronize(c->stream));
-  c->syncs++;
-}
-
-float read_f(flof_ctx *c, const float *dev) {
-  CK(cudaMemcpyAsync(c->fres_h, dev, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-  sync(c);
-  return c->fres_h[0];
-}
-
-int trunc_f(float v) {
-  if (v != v) return 0;
-  if (v >= 2147483647.f) return 2147483647;
-  if (v <= -2147483648.f) return (-2147483647 - 1);
-  return (int)v;
-}
-int trunc_d(double v) {
-  if (v != v) return 0;
-  if (v >= 2147483647.0) return 2147483647;
-  if (v <= -2147483648.0) return (-2147483647 - 1);
-  return (int)v;
-}
-
-// Reads and clears the device error word (after the stream has drained).
-void check_device_errors(flof_ctx *c) {
-  CK(cudaMemcpyAsync(c->fres_h + 9, c->dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  int e = 0;
-  memcpy(&e, c->fres_h + 9, sizeof(int));
-  if (e) {
-    CK(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    fail(FLOF_E_TIMEOUT, "a bounded wait on a TMA copy gave up (device error " +
-                             std::to_string(e) + ")");
-  }
-}
-
-void record_solve(flof_ctx *c, int sx, int iters, float res, int status) {
-  flof_solve_stats *s = c->stats;
-  if (!s) return;
-  if (s->nsolves < FLOF_MAX_SOLVE_STATS) {
-    s->size_x[s->nsolves] = sx;
-    s->iterations[s->nsolves] = iters;
-    s->residual[s->nsolves] = res;
-    s->status[s->nsolves] = status;
-  }
-  s->nsolves++;
-  s->cg_total_iterations += iters > 0 ? iters : 0;
-}
 
 // ---------------------------------------------------------------------------
 // Building blocks of the driver
@@ -723,69 +446,6 @@ float multiscale(flof_ctx *c, Dims4 d, float4 *vel, const float *i0, const float
     errCurr = ls_diff(c, i0warped.f(), i1, nullptr, d, lsDiffFac, resetBnd);
   }
   return errCurr;
-}
-
-// ---------------------------------------------------------------------------
-// C ABI helpers
-// ---------------------------------------------------------------------------
-
-template <class F>
-int guarded(F &&f) {
-  try {
-    f();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) fail(FLOF_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
-    return FLOF_OK;
-  } catch (const FlofError &e) {
-    g_last_error = e.msg;
-    return e.code;
-  } catch (const std::bad_alloc &) {
-    g_last_error = "host allocation failed";
-    return FLOF_E_OOM;
-  } catch (...) {
-    g_last_error = "unknown error";
-    return FLOF_E_CUDA;
-  }
-}
-
-void need(bool cond, const std::string &msg) {
-  if (!cond) fail(FLOF_E_ARG, msg);
-}
-void need_grid(const flof_grid *g, const char *name) {
-  need(g != nullptr, std::string(name) + " is NULL");
-  need(g->d != nullptr || g->cells() == 0, std::string(name) + " has no storage");
-}
-void same_size(const flof_grid *a, const flof_grid *b, const char *what) {
-  need(a->dims[0] == b->dims[0] && a->dims[1] == b->dims[1] && a->dims[2] == b->dims[2] &&
-           a->dims[3] == b->dims[3],
-       std::string(what) + ": different grid resolutions");
-}
-void need_elem(const flof_grid *g, int elem, const char *name) {
-  need(g->elem == elem, std::string(name) + (elem == FLOF_VEC4 ? " must be a Vec4 grid"
-                                                               : " must be a Real grid"));
-}
-void need_4d(const flof_grid *g, const char *name) {
-  for (int q = 0; q < 4; ++q)
-    need(g->dims[q] >= 2, std::string(name) + ": every extent must be at least 2");
-}
-void set_ctx_device(flof_ctx *c) { CK(cudaSetDevice(c->device)); }
-
-float4 f4(const float *v, int nc) {
-  if (!v) return make_float4(0.f, 0.f, 0.f, 0.f);
-  if (nc == 1) return make_float4(v[0], v[0], v[0], v[0]);
-  return make_float4(v[0], v[1], v[2], v[3]);
-}
-
-// gridFactor4d (grid4d.cpp:559-569)
-void grid_factor4d(const float s1[4], const float s2in[4], const float optSize[4],
-                   const float scale[4], float srcFac[4], float retOff[4]) {
-  float s2[4];
-  for (int q = 0; q < 4; ++q) s2[q] = optSize[q] > 0.f ? optSize[q] : s2in[q];
-  for (int q = 0; q < 4; ++q) srcFac[q] = (s1[q] / s2[q]) / scale[q];
-  for (int q = 0; q < 4; ++q) {
-    const float neg = -retOff[q];
-    retOff[q] = neg * srcFac[q] + (float)((double)srcFac[q] * 0.5);
-  }
 }
 
 }  // namespace
