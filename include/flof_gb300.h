@@ -295,6 +295,39 @@ FLOF_API int flof_loadAdvectTimeSlice_OptRunTwoway(
 /* loadAdvectTimeSlice_Finish (optflow4d.cpp:1930-1950). */
 FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *ctx, int id);
 
+/* ---- input conditioning (scenes/flof.py postProcessPhiData :491-531) ---- */
+
+/* repeatFrame4d (optflow4d.cpp:1254-1266): slices int(srct-range+0.5) ..
+ * int(srct) of the bnd box get phi interpolated at time srct.  Slices
+ * outside [0, T) are skipped (the reference does not check). */
+FLOF_API int flof_repeatFrame4d(flof_grid *phi, float srct, float range,
+                                int bnd);
+/* extrap4dLsSimple (optflow4d.cpp:1332-1406) of a Real grid, every extent
+ * at least 3; inside != 0 marches into the positive region. */
+FLOF_API int flof_extrap4dLsSimple(flof_grid *phi, int distance, int inside);
+
+/* ---- 3D Grid<Real> methods of the mode-3 output stage -------------------- */
+/* A 3D grid is a flof_grid with t extent 1; it is 2D when its z extent is
+ * 1, as for the reference's Grid<T>::is3D(). */
+
+/* LevelsetGrid::join (levelset.cpp:114-118): a = min(a, b), any Real grid. */
+FLOF_API int flof_grid_join(flof_grid *a, const flof_grid *b);
+/* Grid<T>::setBound / setBoundNeumann (grid.cpp:462-511) of a 3D grid. */
+FLOF_API int flof_grid3_setBound(flof_grid *a, const float value[4], int w);
+FLOF_API int flof_grid3_setBoundNeumann(flof_grid *a, int w);
+/* simpleBlurSpecial(a, iter, thresh, bord) (test.cpp:94-131) of a 3D Real
+ * grid: the writeResults smoothing and time-SDF merge of scenes/flof.py
+ * (:818-828) and scenes/ofHelpers.py (:108-113). */
+FLOF_API int flof_simpleBlurSpecial(flof_grid *a, int iter, float thresh,
+                                    int bord);
+
+/* ---- hi-res 4D assembly with partial loads (flof.py:707-723) ------------ */
+
+/* shiftForwGrid4d (optflow4d.cpp:1596-1616): t slices [T-good, T) move to
+ * [0, good).  good must be below T (the reference loops forever for
+ * good >= T). */
+FLOF_API int flof_shiftForwGrid4d(flof_grid *phi, int overrideGoodRegion);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,13 @@ SIGNATURES = {
     "flof_loadAdvectTimeSlice_OptRun": (I, [P, I, P, P, F, F, F, P, P, P, P, F, I, F, I, F, F]),
     "flof_loadAdvectTimeSlice_OptRunTwoway": (I, [P, I, I, P, P, P, F, F, F, F, P, P, P, P, F, I, F]),
     "flof_loadAdvectTimeSlice_Finish": (I, [P, I]),
+    "flof_repeatFrame4d": (I, [P, F, F, I]),
+    "flof_extrap4dLsSimple": (I, [P, I, I]),
+    "flof_grid_join": (I, [P, P]),
+    "flof_grid3_setBound": (I, [P, P, I]),
+    "flof_grid3_setBoundNeumann": (I, [P, I]),
+    "flof_simpleBlurSpecial": (I, [P, I, F, I]),
+    "flof_shiftForwGrid4d": (I, [P, I]),
 }
 
 _lib = None

@@ -32,6 +32,7 @@ __all__ = [
     "interpolateGrid4d", "interpolateGrid4dVec", "deform4d",
     "loadAdvectTimeSlice_OptInit", "loadAdvectTimeSlice_OptRun",
     "loadAdvectTimeSlice_OptRunTwoway", "loadAdvectTimeSlice_Finish", "last_solve_stats",
+    "LevelsetGrid", "repeatFrame4d", "extrap4dLsSimple", "simpleBlurSpecial", "shiftForwGrid4d",
 ]
 
 
@@ -251,6 +252,10 @@ class _Grid:
     def setBoundNeumann(self, boundaryWidth=1):
         check(self.ctx.lib.flof_grid_setBoundNeumann(self.h, int(boundaryWidth)))
 
+    def join(self, a):
+        """LevelsetGrid::join (levelset.cpp:114-118): self = min(self, a)."""
+        check(self.ctx.lib.flof_grid_join(self.h, a.h))
+
     def free(self):
         if getattr(self, "h", None) is not None:
             self.ctx.lib.flof_grid_destroy(self.h)
@@ -276,7 +281,9 @@ class Grid4Vec4(_Grid):
 
 
 class RealGrid(_Grid):
-    """A 3D Grid<Real> (t extent 1), the output of the mode-3 slice lookup."""
+    """A 3D Grid<Real> (t extent 1), the output of the mode-3 slice lookup.
+    Its border methods follow Grid<T> (grid.cpp:462-511): the z planes count
+    only when the z extent is above 1."""
     ELEM = FLOF_REAL
     NC = 1
 
@@ -288,6 +295,15 @@ class RealGrid(_Grid):
     def shape(self):
         X, Y, Z, _ = self.dims
         return (Z, Y, X)
+
+    def setBound(self, value, boundaryWidth=1):
+        check(self.ctx.lib.flof_grid3_setBound(self.h, f4(value), int(boundaryWidth)))
+
+    def setBoundNeumann(self, boundaryWidth=1):
+        check(self.ctx.lib.flof_grid3_setBoundNeumann(self.h, int(boundaryWidth)))
+
+
+LevelsetGrid = RealGrid
 
 
 class Solver:
@@ -477,3 +493,27 @@ def loadAdvectTimeSlice_Finish(ID):
         return
     ctx = ent[0]
     check(ctx.lib.flof_loadAdvectTimeSlice_Finish(ctx.h, int(ID)))
+
+
+# ---------------------------------------------------------------------------
+# input conditioning and output stage (scenes/flof.py postProcessPhiData,
+# writeResults and the time-SDF merge)
+# ---------------------------------------------------------------------------
+def repeatFrame4d(phi, srct, range=0.0, bnd=0):
+    """repeatFrame4d (optflow4d.cpp:1254-1266)."""
+    check(phi.ctx.lib.flof_repeatFrame4d(phi.h, float(srct), float(range), int(bnd)))
+
+
+def extrap4dLsSimple(phi, distance=4, inside=False):
+    """extrap4dLsSimple (optflow4d.cpp:1332-1406)."""
+    check(phi.ctx.lib.flof_extrap4dLsSimple(phi.h, int(distance), 1 if inside else 0))
+
+
+def simpleBlurSpecial(a, iter=1, thresh=0.0, bord=0):
+    """simpleBlurSpecial (test.cpp:116-131) of a 3D RealGrid."""
+    check(a.ctx.lib.flof_simpleBlurSpecial(a.h, int(iter), float(thresh), int(bord)))
+
+
+def shiftForwGrid4d(phi, overrideGoodRegion=0):
+    """shiftForwGrid4d (optflow4d.cpp:1596-1616)."""
+    check(phi.ctx.lib.flof_shiftForwGrid4d(phi.h, int(overrideGoodRegion)))

@@ -242,6 +242,34 @@ __device__ __forceinline__ float4 interp3_vec(const float4 *__restrict__ data,
   return r;
 }
 
+// interpol<Real> (source/util/interpol.h:57-95) on a 3D Real grid of extents
+// size[0..2] with z stride sZ: same index build and sum order as
+// interp3_vec.
+__device__ __forceinline__ float interp3_real(const float *__restrict__ data, const int size[3],
+                                              idx_t sZ, float q0, float q1, float q2) {
+  const float px = q0 - 0.5f, py = q1 - 0.5f, pz = q2 - 0.5f;
+  int xi = trunc_i(px), yi = trunc_i(py), zi = trunc_i(pz);
+  float s1 = px - (float)xi, s0 = 1.0f - s1;
+  float t1 = py - (float)yi, t0 = 1.0f - t1;
+  float f1 = pz - (float)zi, f0 = 1.0f - f1;
+  if (px < 0.f) { xi = 0; s0 = 1.f; s1 = 0.f; }
+  if (py < 0.f) { yi = 0; t0 = 1.f; t1 = 0.f; }
+  if (pz < 0.f) { zi = 0; f0 = 1.f; f1 = 0.f; }
+  if (xi >= size[0] - 1) { xi = size[0] - 2; s0 = 0.f; s1 = 1.f; }
+  if (yi >= size[1] - 1) { yi = size[1] - 2; t0 = 0.f; t1 = 1.f; }
+  if (size[2] > 1) {
+    if (zi >= size[2] - 1) { zi = size[2] - 2; f0 = 0.f; f1 = 1.f; }
+  }
+  const idx_t X = 1, Y = size[0], Z = sZ;
+  const idx_t i = (idx_t)xi + Y * yi + Z * zi;
+  return ((__ldg(data + i) * t0 + __ldg(data + i + Y) * t1) * s0 +
+          (__ldg(data + i + X) * t0 + __ldg(data + i + X + Y) * t1) * s1) *
+             f0 +
+         ((__ldg(data + i + Z) * t0 + __ldg(data + i + Y + Z) * t1) * s0 +
+          (__ldg(data + i + X + Z) * t0 + __ldg(data + i + X + Y + Z) * t1) * s1) *
+             f1;
+}
+
 // ---- compensated accumulation ------------------------------------------------
 
 // Float-float accumulator (Knuth's TwoSum): `hi` carries the running sum,

@@ -181,4 +181,25 @@ void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
 void launch_expol_sweep(const float4 *in, float4 *out, const float *mark,
                         Dims4 d, cudaStream_t s);
 
+// ---- input conditioning and output stage (flof_cond.cu) ---------------------
+// repeatFrame4d: slices t0..t1 of the bnd box get phi interpolated at time
+// srct; `slice` is scratch of X*Y*Z floats.
+void launch_repeat_frame(float *phi, Dims4 d, float srct, int t0, int t1, int bnd, float *slice,
+                         cudaStream_t s);
+// extrap4dLsSimple steps; tmp holds X*Y*Z*T ints.
+void launch_extrap_mark(const float *phi, int *tmp, Dims4 d, int inside, cudaStream_t s);
+void launch_extrap_layer(int *tmp, Dims4 d, cudaStream_t s);
+void launch_extrap_step(float *phi, int *tmp, Dims4 d, int dd, float direction, cudaStream_t s);
+void launch_extrap_remaining(float *phi, const int *tmp, Dims4 d, float value, cudaStream_t s);
+// one knSimpleBlurSpecial pass a -> tmp over a 3D (Z > 1) or 2D (Z == 1) grid
+void launch_simple_blur_special(const float *a, float *tmp, int X, int Y, int Z, float thresh,
+                                int bord, cudaStream_t s);
+void launch_join(float *a, const float *b, long long n, cudaStream_t s);
+void launch_set_bound3(float *a, int X, int Y, int Z, int nc, float4 v, int w, cudaStream_t s);
+void launch_set_bound_neumann3(float *a, int X, int Y, int Z, int nc, int w, cudaStream_t s);
+// knLoadPlaceGridIpol / knLoadPlaceGridRescale
+void launch_place_slice(float *phi, Dims4 d, int slice, const float *src, const int sdims[3],
+                        const float sf[3], const float off[3], float wc, cudaStream_t s);
+void launch_rescale_slices(float *phi, Dims4 d, const float *w, cudaStream_t s);
+
 }  // namespace flof

@@ -91,6 +91,12 @@ class Oracle:
             "optRunFrame": (None, [P, P, P, P, P, P, R, R, R, P, P, P, P, R, I, R]),
             "statsReset": (None, []),
             "statsGet": (I, [P, P, P, I]),
+            "repeatFrame4d": (None, [P, P, R, R, I]),
+            "extrap4dLsSimple": (None, [P, P, I, I]),
+            "join": (None, [ctypes.c_longlong, P, P]),
+            "setBound3": (None, [P, P, I, P, I]),
+            "setBoundNeumann3": (None, [P, P, I, I]),
+            "simpleBlurSpecial": (None, [P, P, I, R, I]),
         }
         for name, (res, args) in sig.items():
             fn = self._f(name)
@@ -178,6 +184,51 @@ class Oracle:
     def setBoundNeumann(self, a, w):
         a = self._arr(a).copy()
         self._f("setBoundNeumann")(self._p(self._dims(dims_of(a))), self._p(a), ncomp(a), int(w))
+        return a
+
+    # -- input conditioning ---------------------------------------------------
+    def repeatFrame4d(self, phi, srct, range_=0.0, bnd=0):
+        a = self._arr(phi).copy()
+        self._f("repeatFrame4d")(self._p(self._dims(dims_of(a))), self._p(a), float(srct),
+                                 float(range_), int(bnd))
+        return a
+
+    def extrap4dLsSimple(self, phi, distance=4, inside=False):
+        a = self._arr(phi).copy()
+        self._f("extrap4dLsSimple")(self._p(self._dims(dims_of(a))), self._p(a), int(distance),
+                                    1 if inside else 0)
+        return a
+
+    # -- 3D grids (arrays of shape (Z, Y, X[, 4])) -------------------------------
+    @staticmethod
+    def _dims3(a):
+        z, y, x = a.shape[:3]
+        return np.ascontiguousarray(np.asarray((x, y, z), dtype=np.int32))
+
+    def join(self, a, b):
+        a = self._arr(a).copy()
+        b = self._arr(b)
+        assert a.shape == b.shape
+        self._f("join")(a.size, self._p(a), self._p(b))
+        return a
+
+    def setBound3(self, a, value, w):
+        a = self._arr(a).copy()
+        nc = 4 if a.ndim == 4 else 1
+        self._f("setBound3")(self._p(self._dims3(a)), self._p(a), nc, self._p(self._vec(value, nc)),
+                             int(w))
+        return a
+
+    def setBoundNeumann3(self, a, w):
+        a = self._arr(a).copy()
+        nc = 4 if a.ndim == 4 else 1
+        self._f("setBoundNeumann3")(self._p(self._dims3(a)), self._p(a), nc, int(w))
+        return a
+
+    def simpleBlurSpecial(self, a, iter_=1, thresh=0.0, bord=0):
+        a = self._arr(a).copy()
+        self._f("simpleBlurSpecial")(self._p(self._dims3(a)), self._p(a), int(iter_),
+                                     float(thresh), int(bord))
         return a
 
     # -- resampling ----------------------------------------------------------

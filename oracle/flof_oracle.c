@@ -1382,3 +1382,174 @@ EXPORT void ORC_SYM(optRunFrame)(const int *defoDims, const REAL *defo,
                blendAlpha, vt, defoDims, sf3, off3, df, bordSkip);
   free(vt);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Input conditioning (scenes/flof.py postProcessPhiData :491-531)          */
+/* ------------------------------------------------------------------------ */
+
+/* repeatFrame4d (optflow4d.cpp:1254-1266): serial and in place like the
+ * reference.  The reference does not range-check t; slices outside [0, T)
+ * are skipped here. */
+EXPORT void ORC_SYM(repeatFrame4d)(const int *dims, REAL *phi, REAL srct,
+                                   REAL range, int bnd) {
+  const dims4 d = mkdims(dims);
+  const int t0 = trunc_int_d((double)(srct - range) + 0.5);
+  const int t1 = trunc_int(srct);
+  for (int t = t0; t <= t1; t++) {
+    if (t < 0 || t >= d.t) continue;
+    for (int k = bnd; k < d.z - bnd; ++k)
+      for (int j = bnd; j < d.y - bnd; j++)
+        for (int i = bnd; i < d.x - bnd; i++) {
+          const REAL pos[4] = {(REAL)i + (REAL)0.5, (REAL)j + (REAL)0.5,
+                               (REAL)k + (REAL)0.5, srct + (REAL)0.5};
+          phi[index4(d, i, j, k, t)] = interp4_real(phi, d, pos);
+        }
+  }
+}
+
+/* extrap4dLsSimple (optflow4d.cpp:1332-1406) with its Grid4d<int> marks;
+ * knExtrap4dLsSimple (:1328-1350) and knSetRemaining4d (:1352-1357) run
+ * serially over the bnd = 1 box (both are race-free as parallel kernels: a
+ * sweep reads only cells marked d and writes only cells marked 0). */
+EXPORT void ORC_SYM(extrap4dLsSimple)(const int *dims, REAL *phi, int distance,
+                                      int inside) {
+  const dims4 d = mkdims(dims);
+  const idx_t n = ncell(d);
+  int *tmp = (int *)xcalloc(n, sizeof(int));
+  /* nbs4d (optflow4d.cpp:1323-1326): -x,+x,-y,+y,-z,+z,-t,+t */
+  const idx_t off[8] = {-1, 1, -(idx_t)d.x, (idx_t)d.x, -(idx_t)d.x * d.y,
+                        (idx_t)d.x * d.y, -(idx_t)d.x * d.y * d.z,
+                        (idx_t)d.x * d.y * d.z};
+  REAL direction = 1.;
+  if (inside) direction = -1.;
+  for (int t = 1; t < d.t - 1; ++t)
+    for (int k = 1; k < d.z - 1; ++k)
+      for (int j = 1; j < d.y - 1; ++j)
+        for (int i = 1; i < d.x - 1; ++i) {
+          const idx_t q = index4(d, i, j, k, t);
+          if (!inside ? (phi[q] < 0.) : (phi[q] > 0.)) tmp[q] = 1;
+        }
+  for (int t = 1; t < d.t - 1; ++t)
+    for (int k = 1; k < d.z - 1; ++k)
+      for (int j = 1; j < d.y - 1; ++j)
+        for (int i = 1; i < d.x - 1; ++i) {
+          const idx_t q = index4(d, i, j, k, t);
+          if (tmp[q]) continue;
+          for (int m = 0; m < 8; ++m)
+            if (tmp[q + off[m]] == 1) {
+              tmp[q] = 2;
+              break;
+            }
+        }
+  for (int dd = 2; dd < 1 + distance; ++dd)
+    for (int t = 1; t < d.t - 1; ++t)
+      for (int k = 1; k < d.z - 1; ++k)
+        for (int j = 1; j < d.y - 1; ++j)
+          for (int i = 1; i < d.x - 1; ++i) {
+            const idx_t q = index4(d, i, j, k, t);
+            if (tmp[q] != 0) continue;
+            int nbs = 0;
+            REAL avg = 0.;
+            for (int m = 0; m < 8; ++m)
+              if (tmp[q + off[m]] == dd) {
+                avg += phi[q + off[m]];
+                nbs++;
+              }
+            if (nbs > 0) {
+              tmp[q] = dd + 1;
+              phi[q] = avg / (REAL)nbs + direction;
+            }
+          }
+  for (int t = 1; t < d.t - 1; ++t)
+    for (int k = 1; k < d.z - 1; ++k)
+      for (int j = 1; j < d.y - 1; ++j)
+        for (int i = 1; i < d.x - 1; ++i) {
+          const idx_t q = index4(d, i, j, k, t);
+          if (tmp[q] == 0) phi[q] = (REAL)(direction * (REAL)(distance + 2));
+        }
+  free(tmp);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3D Grid<Real> methods of the mode-3 output stage                          */
+/* ------------------------------------------------------------------------ */
+
+/* LevelsetGrid::join (levelset.cpp:114-118): a = std::min(a, b). */
+EXPORT void ORC_SYM(join)(idx_t n, REAL *a, const REAL *b) {
+  for (idx_t q = 0; q < n; ++q) a[q] = (b[q] < a[q]) ? b[q] : a[q];
+}
+
+/* Grid<T>::setBound (grid.cpp:462-473) of a 3D grid (dims3 = X, Y, Z). */
+EXPORT void ORC_SYM(setBound3)(const int *dims3, REAL *a, int nc, const REAL *v,
+                               int w) {
+  const int X = dims3[0], Y = dims3[1], Z = dims3[2];
+  const int is3d = Z > 1;
+  for (int k = 0; k < Z; ++k)
+    for (int j = 0; j < Y; ++j)
+      for (int i = 0; i < X; ++i) {
+        const int b = (i <= w || i >= X - 1 - w || j <= w || j >= Y - 1 - w ||
+                       (is3d && (k <= w || k >= Z - 1 - w)));
+        if (!b) continue;
+        const idx_t q = (idx_t)i + (idx_t)X * j + (idx_t)X * Y * k;
+        for (int c = 0; c < nc; ++c) a[q * nc + c] = v[c];
+      }
+}
+
+/* Grid<T>::setBoundNeumann (grid.cpp:475-511) of a 3D grid. */
+EXPORT void ORC_SYM(setBoundNeumann3)(const int *dims3, REAL *a, int nc, int w) {
+  const int X = dims3[0], Y = dims3[1], Z = dims3[2];
+  const int is3d = Z > 1;
+  for (int k = 0; k < Z; ++k)
+    for (int j = 0; j < Y; ++j)
+      for (int i = 0; i < X; ++i) {
+        int set = 0, si = i, sj = j, sk = k;
+        if (i <= w) { si = w + 1; set = 1; }
+        if (i >= X - 1 - w) { si = X - 1 - w - 1; set = 1; }
+        if (j <= w) { sj = w + 1; set = 1; }
+        if (j >= Y - 1 - w) { sj = Y - 1 - w - 1; set = 1; }
+        if (is3d) {
+          if (k <= w) { sk = w + 1; set = 1; }
+          if (k >= Z - 1 - w) { sk = Z - 1 - w - 1; set = 1; }
+        }
+        if (!set) continue;
+        const idx_t q = (idx_t)i + (idx_t)X * j + (idx_t)X * Y * k;
+        const idx_t s = (idx_t)si + (idx_t)X * sj + (idx_t)X * Y * sk;
+        for (int c = 0; c < nc; ++c) a[q * nc + c] = a[s * nc + c];
+      }
+}
+
+/* simpleBlurSpecial / knSimpleBlurSpecial (test.cpp:94-131) of a 3D grid:
+ * `iter` passes into a fresh zeroed grid with a swap after each. */
+EXPORT void ORC_SYM(simpleBlurSpecial)(const int *dims3, REAL *a, int iter,
+                                       REAL thresh, int bord) {
+  const int X = dims3[0], Y = dims3[1], Z = dims3[2];
+  const int is3d = Z > 1;
+  const idx_t n = (idx_t)X * Y * Z, sY = X, sZ = (idx_t)X * Y;
+  REAL *tmp = (REAL *)xcalloc(n, sizeof(REAL));
+  REAL *cur = a, *nxt = tmp;
+  for (int it = 0; it < iter; ++it) {
+    for (int k = is3d ? 1 : 0; k < (is3d ? Z - 1 : 1); ++k)
+      for (int j = 1; j < Y - 1; ++j)
+        for (int i = 1; i < X - 1; ++i) {
+          const idx_t q = (idx_t)i + sY * j + sZ * k;
+          int inb = i >= bord && j >= bord && i < X - bord && j < Y - bord;
+          inb = inb && (is3d ? (k >= bord && k < Z - bord) : (k == 0));
+          if (!inb || cur[q] < thresh) {
+            nxt[q] = cur[q];
+            continue;
+          }
+          nxt[q] = cur[q + 1] + cur[q - 1] + cur[q + sY] + cur[q - sY];
+          if (is3d) {
+            nxt[q] += cur[q + sZ] + cur[q - sZ];
+            nxt[q] = (REAL)((double)nxt[q] * (1. / 6.));
+          } else {
+            nxt[q] = (REAL)((double)nxt[q] * (1. / 4.));
+          }
+        }
+    REAL *sw = cur;
+    cur = nxt;
+    nxt = sw;
+  }
+  if (cur != a) memcpy(a, cur, (size_t)n * sizeof(REAL));
+  free(tmp);
+}
