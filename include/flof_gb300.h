@@ -295,6 +295,24 @@ FLOF_API int flof_loadAdvectTimeSlice_OptRunTwoway(
 /* loadAdvectTimeSlice_Finish (optflow4d.cpp:1930-1950). */
 FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *ctx, int id);
 
+/* ---- .uni grid files (source/fileio.cpp:834-1000) ------------------------
+ * gzip streams: a 4-byte tag ("MNT2" 3D, "M4T2" 4D), the 288-byte UniHeader,
+ * for 4D an int32 t extent, then float32 cells x fastest.  zlib is loaded at
+ * run time (libz.so.1). */
+
+/* Header of a file: dims = x, y, z, t (t = 1 for a 3D file). */
+FLOF_API int flof_uni_info(const char *fname, int dims[4], int *is4d,
+                           int *gridType, int *bytesPerElement);
+/* Grid4d::load / Grid<T>::load: the file's extents and element size must
+ * match the grid (a 3D file needs t extent 1). */
+FLOF_API int flof_grid_load(flof_grid *grid, const char *fname);
+/* Grid4d::save (is4d != 0, M4T2) / Grid<Real>::save (is4d == 0, MNT2). */
+FLOF_API int flof_grid_save(const flof_grid *grid, const char *fname,
+                            int is4d);
+/* readGrid4dUni(name, NULL, t, slice) (fileio.cpp:912-990): t slice of a 4D
+ * file into a grid with the file's x, y, z extents and t extent 1. */
+FLOF_API int flof_uni_read_slice(flof_grid *slice, const char *fname, int t);
+
 /* ---- input conditioning (scenes/flof.py postProcessPhiData :491-531) ---- */
 
 /* repeatFrame4d (optflow4d.cpp:1254-1266): slices int(srct-range+0.5) ..
@@ -327,6 +345,45 @@ FLOF_API int flof_simpleBlurSpecial(flof_grid *a, int iter, float thresh,
  * [0, good).  good must be below T (the reference loops forever for
  * good >= T). */
 FLOF_API int flof_shiftForwGrid4d(flof_grid *phi, int overrideGoodRegion);
+/* loadPlaceGrid4d (optflow4d.cpp:1460-1594): places the 3D slice files
+ * fname % fileid (a printf pattern with one integer conversion; .uni MNT2)
+ * into the Real 4D grid phi.  With fname NULL the slices are the device
+ * grids slices[fileid - fileIdxStart], q < nslices.  Vector arguments are
+ * float[4]; overrideSize may be NULL. */
+FLOF_API int flof_loadPlaceGrid4d(flof_grid *phi, const char *fname,
+                                  const flof_grid *const *slices, int nslices,
+                                  const float offset[4], const float scale[4],
+                                  int fileIdxStart, int fileIdxEnd,
+                                  int debugSkipLoad, float spread,
+                                  const float overrideSize[4],
+                                  float overrideTimeOff, int overrideGoodRegion,
+                                  float loadTimeScale, int rescaleSdfValues,
+                                  float sdfIsoOff, float repeatStartFrame);
+
+/* ---- mode 3 from files ---------------------------------------------------- */
+
+/* loadAdvectTimeSlice_OptInit with the reference's file argument: the M4T2
+ * Vec4 deformation file is loaded whole into device memory owned by the
+ * context until Finish. */
+FLOF_API int flof_loadAdvectTimeSlice_OptInitFile(flof_ctx *ctx, int id,
+                                                  const char *fname,
+                                                  int useDefoVols,
+                                                  int doAligned,
+                                                  float partialLoadFac);
+/* loadAdvectTimeSlice (optflow4d.cpp:1671-1760), the non-optimised twin of
+ * OptRun: blends deformation slices t and t+1 of `defo` (device Vec4 grid)
+ * or, when defo is NULL, of the file fname, and looks phi up over the
+ * bnd = 1 box of dst (no bordSkip, as in the reference). */
+FLOF_API int flof_loadAdvectTimeSlice(flof_ctx *ctx, const flof_grid *defo,
+                                      const char *fname, flof_grid *dst,
+                                      const flof_grid *phi, float time,
+                                      float blendAlpha, float loadTimeScale,
+                                      const float defoOffset[4],
+                                      const float defoScale[4],
+                                      const float defoFactor[4],
+                                      const float overrideSize[4],
+                                      float overrideTimeOff, int zeroVel,
+                                      float defoAniFac);
 
 #ifdef __cplusplus
 }

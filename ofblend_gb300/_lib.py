@@ -135,6 +135,13 @@ SIGNATURES = {
     "flof_grid3_setBoundNeumann": (I, [P, I]),
     "flof_simpleBlurSpecial": (I, [P, I, F, I]),
     "flof_shiftForwGrid4d": (I, [P, I]),
+    "flof_loadPlaceGrid4d": (I, [P, ctypes.c_char_p, P, I, P, P, I, I, I, F, P, F, I, F, I, F, F]),
+    "flof_uni_info": (I, [ctypes.c_char_p, P, IP, IP, IP]),
+    "flof_grid_load": (I, [P, ctypes.c_char_p]),
+    "flof_grid_save": (I, [P, ctypes.c_char_p, I]),
+    "flof_uni_read_slice": (I, [P, ctypes.c_char_p, I]),
+    "flof_loadAdvectTimeSlice_OptInitFile": (I, [P, I, ctypes.c_char_p, I, I, F]),
+    "flof_loadAdvectTimeSlice": (I, [P, P, ctypes.c_char_p, P, P, F, F, F, P, P, P, P, F, I, F]),
 }
 
 _lib = None

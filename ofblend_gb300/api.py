@@ -18,11 +18,12 @@ exceptions surface as Python errors.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
 from . import _lib
-from ._lib import FLOF_REAL, FLOF_VEC4, FlofError, OFParams, SolveStats, check, f4
+from ._lib import FLOF_REAL, FLOF_VEC4, FlofError, OFParams, SolveStats, check, f4, lib
 
 __all__ = [
     "FlofError", "Context", "context", "Solver", "Grid4Real", "Grid4Vec4", "RealGrid",
@@ -33,6 +34,7 @@ __all__ = [
     "loadAdvectTimeSlice_OptInit", "loadAdvectTimeSlice_OptRun",
     "loadAdvectTimeSlice_OptRunTwoway", "loadAdvectTimeSlice_Finish", "last_solve_stats",
     "LevelsetGrid", "repeatFrame4d", "extrap4dLsSimple", "simpleBlurSpecial", "shiftForwGrid4d",
+    "uniFileInfo", "getUniFileSize", "readGrid4dUniSlice", "loadPlaceGrid4d", "loadAdvectTimeSlice",
 ]
 
 
@@ -256,6 +258,16 @@ class _Grid:
         """LevelsetGrid::join (levelset.cpp:114-118): self = min(self, a)."""
         check(self.ctx.lib.flof_grid_join(self.h, a.h))
 
+    # -- .uni files (fileio.cpp:834-1000) -----------------------------------------
+    def load(self, name):
+        """Grid4d::load / Grid<T>::load of a .uni file."""
+        check(self.ctx.lib.flof_grid_load(self.h, os.fsencode(name)))
+        return self
+
+    def save(self, name):
+        """Grid4d::save (M4T2) / Grid<Real>::save (MNT2)."""
+        check(self.ctx.lib.flof_grid_save(self.h, os.fsencode(name), 0 if self._is3d() else 1))
+
     def free(self):
         if getattr(self, "h", None) is not None:
             self.ctx.lib.flof_grid_destroy(self.h)
@@ -443,11 +455,20 @@ def deform4d(out, i0, i1, vel, velInv=None, alpha=1.0, twoway=1):
                                 int(twoway)))
 
 
-def loadAdvectTimeSlice_OptInit(ID, fname1, useDefoVols=False, doAligned=False, partialLoadFac=0.2):
+def loadAdvectTimeSlice_OptInit(ID, fname1, useDefoVols=False, doAligned=False, partialLoadFac=0.2,
+                                ctx: Context | None = None):
     """loadAdvectTimeSlice_OptInit (optflow4d.cpp:1871-1913).  `fname1` is the
-    deformation as a GPU-resident Grid4Vec4 instead of a .uni file name."""
+    .uni deformation file (loaded whole into device memory) or a GPU-resident
+    Grid4Vec4."""
+    if isinstance(fname1, (str, os.PathLike)):
+        ctx = ctx or context()
+        check(ctx.lib.flof_loadAdvectTimeSlice_OptInitFile(
+            ctx.h, int(ID), os.fsencode(fname1), int(bool(useDefoVols)), int(bool(doAligned)),
+            float(partialLoadFac)))
+        _lats_ctx[int(ID)] = (ctx, None)
+        return
     if not isinstance(fname1, Grid4Vec4):
-        raise FlofError(1, "loadAdvectTimeSlice_OptInit expects the deformation as a Grid4Vec4")
+        raise FlofError(1, "loadAdvectTimeSlice_OptInit expects a file name or a Grid4Vec4")
     ctx = fname1.ctx
     check(ctx.lib.flof_loadAdvectTimeSlice_OptInit(ctx.h, int(ID), fname1.h, int(bool(useDefoVols)),
                                                    int(bool(doAligned)), float(partialLoadFac)))
@@ -517,3 +538,68 @@ def simpleBlurSpecial(a, iter=1, thresh=0.0, bord=0):
 def shiftForwGrid4d(phi, overrideGoodRegion=0):
     """shiftForwGrid4d (optflow4d.cpp:1596-1616)."""
     check(phi.ctx.lib.flof_shiftForwGrid4d(phi.h, int(overrideGoodRegion)))
+
+
+# ---------------------------------------------------------------------------
+# .uni files, hi-res 4D assembly, non-optimised slice lookup
+# ---------------------------------------------------------------------------
+def uniFileInfo(name) -> dict:
+    """Header of a .uni file: dims (x, y, z, t), 4D flag, grid type, element size."""
+    L = lib()
+    dims = (ctypes.c_int * 4)()
+    is4d, gt, bpe = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(L.flof_uni_info(os.fsencode(name), dims, ctypes.byref(is4d), ctypes.byref(gt), ctypes.byref(bpe)))
+    return {"dims": tuple(dims), "is4d": bool(is4d.value), "gridType": gt.value,
+            "bytesPerElement": bpe.value}
+
+
+def getUniFileSize(name):
+    """getUniFileSize (fileio.cpp:572-604) as a vec3."""
+    d = uniFileInfo(name)["dims"]
+    return vec3(d[0], d[1], d[2])
+
+
+def readGrid4dUniSlice(name, t, slice_grid):
+    """readGrid4dUni(name, NULL, t, slice) (fileio.cpp:912-990): t slice of a
+    4D file into a grid with t extent 1."""
+    check(slice_grid.ctx.lib.flof_uni_read_slice(slice_grid.h, os.fsencode(name), int(t)))
+    return slice_grid
+
+
+def loadPlaceGrid4d(fname, phi, offset, scale, fileIdxStart=-1, fileIdxEnd=-1, debugSkipLoad=999999,
+                    spread=1.0, overrideSize=None, overrideTimeOff=0.0, overrideGoodRegion=0,
+                    loadTimeScale=1.0, rescaleSdfValues=False, sdfIsoOff=0.0, repeatStartFrame=0.0):
+    """loadPlaceGrid4d (optflow4d.cpp:1460-1594).  `fname` is a file-name
+    pattern with one integer conversion (3D .uni files) or a list of RealGrid
+    slices, element q holding file index fileIdxStart + q."""
+    L = phi.ctx.lib
+    if isinstance(fname, (str, os.PathLike)):
+        name, arr, n = os.fsencode(fname), None, 0
+    else:
+        grids = list(fname)
+        arr = (ctypes.c_void_p * len(grids))(*[g.h.value for g in grids])
+        name, n = None, len(grids)
+    check(L.flof_loadPlaceGrid4d(
+        phi.h, name, arr, n, f4(offset), f4(scale), int(fileIdxStart), int(fileIdxEnd), int(debugSkipLoad),
+        float(spread), f4(overrideSize if overrideSize is not None else -1.0), float(overrideTimeOff),
+        int(overrideGoodRegion), float(loadTimeScale), int(bool(rescaleSdfValues)), float(sdfIsoOff),
+        float(repeatStartFrame)))
+
+
+def loadAdvectTimeSlice(dummyID, fname, dst, phi, time, blendAlpha, loadTimeScale, defoOffset, defoScale,
+                        defoFactor, overrideSize=None, overrideTimeOff=0.0, debugVel=None, debugVelT=None,
+                        zeroVel=False, thirdAlpha=0.0, bordSkip=1, fourthAlpha=0.0, defoAniFac=1.0):
+    """loadAdvectTimeSlice (optflow4d.cpp:1671-1760), the non-optimised twin of
+    OptRun.  `fname` is the .uni deformation file or a Grid4Vec4; debugVel /
+    debugVelT outputs are not offered (they must be None)."""
+    if debugVel is not None or debugVelT is not None:
+        raise FlofError(1, "debugVel / debugVelT outputs are not supported")
+    ctx = dst.ctx
+    if isinstance(fname, (str, os.PathLike)):
+        defo, name = None, os.fsencode(fname)
+    else:
+        defo, name = fname.h, None
+    check(ctx.lib.flof_loadAdvectTimeSlice(
+        ctx.h, defo, name, dst.h, phi.h, float(time), float(blendAlpha), float(loadTimeScale),
+        f4(defoOffset), f4(defoScale), f4(defoFactor), f4(overrideSize if overrideSize is not None else -1.0),
+        float(overrideTimeOff), int(bool(zeroVel)), float(defoAniFac)))

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflof_gb300.so")
 SOURCES = ["flof_ops.cu", "flof_solve.cu", "flof_stencil.cu", "flof_tma.cu", "flof_cond.cu",
-           "flof_host.cu", "flof_ext.cu", "flof_noalloc.cu"]
+           "flof_host.cu", "flof_ext.cu", "flof_uni.cu", "flof_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -70,7 +70,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
-        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fPIC"]
+        cmd = [cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fPIC", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

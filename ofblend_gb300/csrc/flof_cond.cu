@@ -268,6 +268,21 @@ __global__ void k_place_slice(float *__restrict__ phi, Dims4 d, int slice,
   }
 }
 
+// tmp(i,j,k) += v over the bnd = 1 box of a 3D grid (the sdfIsoOff fix-up of
+// loadPlaceGrid4d, optflow4d.cpp:1566-1572).
+__global__ void k_add_inner3(float *__restrict__ a, int X, int Y, int Z, float v, Box3 bx,
+                             uint32_t n) {
+  const bool is3d = Z > 1;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    int i, j, k;
+    bx.decode(q, i, j, k);
+    i += 1;
+    j += 1;
+    if (is3d) k += 1;
+    a[(idx_t)i + (idx_t)X * j + (idx_t)X * Y * k] += v;
+  }
+}
+
 // knLoadPlaceGridRescale: phi(i,j,k,t) *= w[t] where w[t] > 0, bnd = 1 box.
 __global__ void k_rescale_slices(float *__restrict__ phi, Dims4 d, const float *__restrict__ w,
                                  BoxDecoder bx, uint32_t n) {
@@ -353,6 +368,13 @@ void launch_place_slice(float *phi, Dims4 d, int slice, const float *src, const 
                                                make_float3(sf[0], sf[1], sf[2]),
                                                make_float3(off[0], off[1], off[2]), wc,
                                                box3(ex, ey), n);
+}
+
+void launch_add_inner3(float *a, int X, int Y, int Z, float v, cudaStream_t s) {
+  const int ex = X - 2, ey = Y - 2, ez = Z > 1 ? Z - 2 : 1;
+  if (ex <= 0 || ey <= 0 || ez <= 0) return;
+  const uint32_t n = (uint32_t)((long long)ex * ey * ez);
+  k_add_inner3<<<grid_for(n, NT), NT, 0, s>>>(a, X, Y, Z, v, box3(ex, ey), n);
 }
 
 void launch_rescale_slices(float *phi, Dims4 d, const float *w, cudaStream_t s) {

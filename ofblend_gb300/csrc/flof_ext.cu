@@ -14,6 +14,39 @@ void need_3d(const flof_grid *g, const char *name) {
   need(g->dims[3] == 1, std::string(name) + " must be a 3D grid (t extent 1)");
 }
 
+// snprintf(pattern, idx) for a file-name pattern with at most one integer
+// conversion (%d, %i, with flags and width) and %% escapes; anything else in
+// a conversion is rejected rather than handed to printf.
+std::string file_name(const char *pattern, int idx) {
+  std::string out;
+  int convs = 0;
+  for (const char *p = pattern; *p; ++p) {
+    if (*p != '%') {
+      out += *p;
+      continue;
+    }
+    if (p[1] == '%') {
+      out += '%';
+      ++p;
+      continue;
+    }
+    const char *q = p + 1;
+    std::string spec = "%";
+    while (*q == '0' || *q == '-' || *q == '+' || *q == ' ') spec += *q++;
+    while (*q >= '0' && *q <= '9') spec += *q++;
+    need(*q == 'd' || *q == 'i', std::string("file name pattern '") + pattern +
+                                     "': only one integer conversion (%d) is supported");
+    need(++convs == 1, std::string("file name pattern '") + pattern +
+                           "' has more than one conversion");
+    spec += 'd';
+    char buf[64];
+    snprintf(buf, sizeof(buf), spec.c_str(), idx);
+    out += buf;
+    p = q;
+  }
+  return out;
+}
+
 }  // namespace
 
 // repeatFrame4d (source/plugin/optflow4d.cpp:1254-1266).  The reference loops
@@ -159,5 +192,145 @@ FLOF_API int flof_shiftForwGrid4d(flof_grid *phi, int overrideGoodRegion) {
       CK(cudaMemcpyAsync(base + (size_t)s * slice, base + (size_t)(s + shift) * slice,
                          (size_t)len * slice, cudaMemcpyDeviceToDevice, phi->ctx->stream));
     }
+  });
+}
+
+// loadPlaceGrid4d (source/plugin/optflow4d.cpp:1460-1594): builds the hi-res
+// 4D level set from a sequence of 3D slice files.  File fileid goes to the
+// t slices around dstt = offset.t + overrideTimeOff + duration * (fileid -
+// fileIdxStart) with hat weights; each placed slice is the trilinear
+// resample of the file to phi's x, y, z extent (bnd = 1 box), and the
+// accumulated weights are divided out at the end.  The slices come from the
+// files fname % fileid (.uni MNT2) or, when fname is NULL, from the device
+// grids slices[fileid - fileIdxStart].
+FLOF_API int flof_loadPlaceGrid4d(flof_grid *phi, const char *fname,
+                                  const flof_grid *const *slices, int nslices,
+                                  const float offset[4], const float scale[4], int fileIdxStart,
+                                  int fileIdxEnd, int debugSkipLoad, float spread,
+                                  const float overrideSize[4], float overrideTimeOff,
+                                  int overrideGoodRegion, float loadTimeScale,
+                                  int rescaleSdfValues, float sdfIsoOff, float repeatStartFrame) {
+  return guarded([&] {
+    need_grid(phi, "phi");
+    need_elem(phi, FLOF_REAL, "phi");
+    need(fname != nullptr || (slices != nullptr && nslices > 0),
+         "either fname or a list of slice grids is required");
+    need(offset != nullptr && scale != nullptr, "offset and scale are required");
+    const Dims4 d = phi->D();
+    need(d.x >= 3 && d.y >= 3 && d.z >= 3 && d.t >= 3,
+         "loadPlaceGrid4d: every extent of phi must be at least 3");
+    flof_ctx *c = phi->ctx;
+    set_ctx_device(c);
+    int sd[3];
+    if (fname) {
+      // the reference probes the size with the raw fileIdxStart
+      const std::string first = file_name(fname, fileIdxStart);
+      const UniInfo u = uni_info(first.c_str());
+      need(!u.is4d && u.bytesPerElement == 4,
+           first + " is not a 3D Real (MNT2) file");
+      sd[0] = u.dims[0];
+      sd[1] = u.dims[1];
+      sd[2] = u.dims[2];
+    } else {
+      for (int q = 0; q < nslices; ++q) {
+        need_grid(slices[q], "slice");
+        need_elem(slices[q], FLOF_REAL, "slice");
+        need_3d(slices[q], "slice");
+        need(q == 0 || (slices[q]->dims[0] == slices[0]->dims[0] &&
+                        slices[q]->dims[1] == slices[0]->dims[1] &&
+                        slices[q]->dims[2] == slices[0]->dims[2]),
+             "all slices must have the same size");
+      }
+      for (int q = 0; q < 3; ++q) sd[q] = slices[0]->dims[q];
+    }
+    need(sd[0] >= 2 && sd[1] >= 2 && sd[2] >= 1, "Invalid src size of the slices");
+    const float v1[4] = {(float)sd[0], (float)sd[1], (float)sd[2], 1.f};
+    float defoSize[4] = {(float)d.x, (float)d.y, (float)d.z, (float)d.t};
+    if (overrideSize && overrideSize[0] > 0.f)
+      for (int q = 0; q < 4; ++q) defoSize[q] = overrideSize[q];
+    float sf[4], off2[4];
+    const float neg1[4] = {-1, -1, -1, -1};
+    for (int q = 0; q < 4; ++q) off2[q] = offset[q];
+    grid_factor4d(v1, defoSize, neg1, scale, sf, off2);
+    const float sf3[3] = {sf[0], sf[1], sf[2]}, off3[3] = {off2[0], off2[1], off2[2]};
+    float valueScale = 1.f;
+    if (rescaleSdfValues) valueScale = (float)(1. / (double)sf[0]);
+    std::vector<float> w(d.t, 0.f);
+    const size_t sliceBytes = (size_t)d.x * d.y * d.z * sizeof(float);
+    if (overrideGoodRegion <= 0) {
+      CK(cudaMemsetAsync(phi->d, 0, phi->bytes(), c->stream));
+    } else if (overrideGoodRegion < d.t) {
+      CK(cudaMemsetAsync((char *)phi->d + sliceBytes * overrideGoodRegion, 0,
+                         sliceBytes * (d.t - overrideGoodRegion), c->stream));
+    }
+    if (fileIdxStart < 0) fileIdxStart = 0;
+    if (fileIdxEnd < 0) fileIdxEnd = trunc_f(defoSize[3]);
+    int repeatOff = 0;
+    if (repeatStartFrame > 0.f)
+      repeatOff = trunc_d((double)((float)(fileIdxEnd - fileIdxStart) * repeatStartFrame) + 1.0);
+    const size_t n3 = (size_t)sd[0] * sd[1] * sd[2];
+    DBuf tmp(c, n3 * sizeof(float));
+    flof_grid tg;
+    tg.ctx = c;
+    tg.dims[0] = sd[0];
+    tg.dims[1] = sd[1];
+    tg.dims[2] = sd[2];
+    tg.dims[3] = 1;
+    tg.elem = FLOF_REAL;
+    tg.d = tmp.p;
+    tg.owned = false;
+    const int endId = fileIdxEnd < debugSkipLoad ? fileIdxEnd : debugSkipLoad;
+    for (int fileid = fileIdxStart - repeatOff; fileid < endId; ++fileid) {
+      const int fileidClamp = fileid > fileIdxStart ? fileid : fileIdxStart;
+      bool didLoad = false;
+      const float duration = (float)(1. * (double)(defoSize[3] * scale[3] / loadTimeScale) /
+                                     (double)(float)(fileIdxEnd - fileIdxStart));
+      const float dstt = offset[3] + overrideTimeOff + duration * (float)(fileid - fileIdxStart);
+      const int s0 = trunc_f(dstt - spread * duration) + 0;
+      const int s1 = trunc_f(dstt + spread * duration) + 2;
+      for (int slice = s0; slice < s1; ++slice) {
+        if (slice < overrideGoodRegion || slice >= d.t) continue;
+        const float q = fabsf((float)slice - dstt) / (duration * spread);
+        const float wc = (float)(1. - (double)q);
+        if (wc < 1e-6f) continue;
+        w[slice] += wc;
+        if (!didLoad) {
+          if (fname) {
+            const std::string nm = file_name(fname, fileidClamp);
+            uni_load(&tg, nm.c_str());
+          } else {
+            const int qi = fileidClamp - fileIdxStart;
+            need(qi >= 0 && qi < nslices,
+                 "loadPlaceGrid4d: no slice grid for file index " + std::to_string(fileidClamp));
+            CK(cudaMemcpyAsync(tmp.p, slices[qi]->d, n3 * sizeof(float),
+                               cudaMemcpyDeviceToDevice, c->stream));
+          }
+          if (rescaleSdfValues && sdfIsoOff != 0.f) {
+            KLP(c, KC_ELEMWISE, sd[0], (double)n3 * 8,
+                launch_add_inner3(tmp.f(), sd[0], sd[1], sd[2], sdfIsoOff, c->stream));
+            KLP(c, KC_BORDER, sd[0], 0,
+                launch_set_bound3(tmp.f(), sd[0], sd[1], sd[2], 1,
+                                  make_float4(1.f, 1.f, 1.f, 1.f), 1, c->stream));
+          }
+          didLoad = true;
+        }
+        KLP(c, KC_RESAMPLE, d.x, (double)d.x * d.y * d.z * 8,
+            launch_place_slice(phi->f(), d, slice, tmp.f(), sd, sf3, off3, wc, c->stream));
+      }
+    }
+    for (int t = 0; t < d.t; ++t) {
+      if (w[t] < 1e-03f) {
+        w[t] = 0.f;
+      } else {
+        w[t] = (float)(1. / (double)w[t]);
+        w[t] *= valueScale;
+      }
+    }
+    DBuf wd(c, (size_t)d.t * sizeof(float));
+    CK(cudaMemcpyAsync(wd.p, w.data(), (size_t)d.t * sizeof(float), cudaMemcpyHostToDevice,
+                       c->stream));
+    KLP(c, KC_ELEMWISE, d.x, (double)d.cells() * 8,
+        launch_rescale_slices(phi->f(), d, wd.f(), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
   });
 }

@@ -1176,6 +1176,34 @@ FLOF_API int flof_loadAdvectTimeSlice_OptInit(flof_ctx *c, int id, const flof_gr
   });
 }
 
+// OptInit with the deformation named by a .uni file (the reference's call):
+// the whole file is loaded into a device grid that the context owns and
+// frees at Finish.
+FLOF_API int flof_loadAdvectTimeSlice_OptInitFile(flof_ctx *c, int id, const char *fname,
+                                                  int useDefoVols, int doAligned,
+                                                  float partialLoadFac) {
+  flof_grid *g = nullptr;
+  const int st = guarded([&] {
+    need(c != nullptr && fname != nullptr, "NULL argument");
+    need(!useDefoVols, "deformation volumes (useDefoVols) are not supported");
+    const UniInfo u = uni_info(fname);
+    need(u.is4d && u.bytesPerElement == 16,
+         std::string(fname) + " is not a 4D Vec4 (M4T2) deformation file");
+    const int dims[4] = {u.dims[0], u.dims[1], u.dims[2], u.dims[3]};
+    if (flof_grid_create(c, dims, FLOF_VEC4, &g) != FLOF_OK) fail(FLOF_E_OOM, g_last_error);
+    uni_load(g, fname);
+  });
+  if (st != FLOF_OK) {
+    if (g) flof_grid_destroy(g);
+    return st;
+  }
+  const int st2 = flof_loadAdvectTimeSlice_OptInit(c, id, g, useDefoVols, doAligned,
+                                                   partialLoadFac);
+  // OptInit pinned g; the destroy is deferred until Finish unpins it
+  flof_grid_destroy(g);
+  return st2;
+}
+
 FLOF_API int flof_loadAdvectTimeSlice_Finish(flof_ctx *c, int id) {
   return guarded([&] {
     need(c != nullptr, "ctx is NULL");
@@ -1280,6 +1308,88 @@ FLOF_API int flof_loadAdvectTimeSlice_OptRun(
                               L.defo->dims[2], make_float4(S.sf[0], S.sf[1], S.sf[2], 0.f),
                               make_float4(S.off2[0], S.off2[1], S.off2[2], 0.f), df, bordSkip,
                               c->stream));
+  });
+}
+
+// loadAdvectTimeSlice (optflow4d.cpp:1671-1760), the non-optimised twin of
+// OptRun: the deformation comes from `defo` (device Vec4 grid) or, when defo
+// is NULL, from slices t and t+1 of the .uni file fname; the lookup covers
+// the bnd = 1 box of dst (bordSkip and thirdAlpha are not supported by the
+// reference either).
+FLOF_API int flof_loadAdvectTimeSlice(flof_ctx *c, const flof_grid *defo, const char *fname,
+                                      flof_grid *dst, const flof_grid *phi, float time,
+                                      float blendAlpha, float loadTimeScale,
+                                      const float defoOffset[4], const float defoScale[4],
+                                      const float defoFactor[4], const float overrideSize[4],
+                                      float overrideTimeOff, int zeroVel, float defoAniFac) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need(defo != nullptr || fname != nullptr, "either defo or fname is required");
+    need_grid(dst, "dst");
+    need_grid(phi, "phi");
+    need_elem(dst, FLOF_REAL, "dst");
+    need_elem(phi, FLOF_REAL, "phi");
+    need(dst->dims[3] == 1, "dst must be a 3D grid (t extent 1)");
+    need_4d(phi, "phi");
+    set_ctx_device(c);
+    // a stand-in grid with the deformation's extents (file mode) for the
+    // size arithmetic
+    flof_grid shape;
+    if (defo) {
+      need_grid(defo, "defo");
+      need_elem(defo, FLOF_VEC4, "defo");
+      shape = *defo;
+    } else {
+      const UniInfo u = uni_info(fname);
+      need(u.is4d && u.bytesPerElement == 16,
+           std::string(fname) + " is not a 4D Vec4 (M4T2) deformation file");
+      memcpy(shape.dims, u.dims, sizeof(shape.dims));
+      shape.elem = FLOF_VEC4;
+      shape.ctx = c;
+    }
+    need(shape.dims[0] >= 2 && shape.dims[1] >= 2 && shape.dims[2] >= 2,
+         "Invalid src size of the deformation");
+    const SliceSetup S =
+        slice_setup(&shape, phi, time, loadTimeScale, defoOffset, defoScale, overrideSize);
+    const long long slice = (long long)shape.dims[0] * shape.dims[1] * shape.dims[2];
+    DBuf vt(c, slice * sizeof(float4));
+    const float4 *v1, *v2;
+    DBuf s1, s2;
+    if (defo) {
+      v1 = defo->v() + (long long)S.t * slice;
+      v2 = defo->v() + (long long)S.tp1 * slice;
+    } else {
+      // readGrid4dUni(fname, NULL, t, &v1) and (.., tp1, &v2)
+      s1 = DBuf(c, slice * sizeof(float4));
+      s2 = DBuf(c, slice * sizeof(float4));
+      flof_grid g1 = shape, g2 = shape;
+      g1.dims[3] = g2.dims[3] = 1;
+      g1.d = s1.p;
+      g2.d = s2.p;
+      g1.owned = g2.owned = false;
+      uni_read_slice(&g1, fname, S.t);
+      uni_read_slice(&g2, fname, S.tp1);
+      v1 = s1.v();
+      v2 = s2.v();
+    }
+    if (zeroVel) {
+      CK(cudaMemsetAsync(vt.p, 0, slice * sizeof(float4), c->stream));
+    } else {
+      KLP(c, KC_BLEND, shape.dims[0], slice * 48,
+          launch_blend_slices(v1, v2, vt.v(), slice, 1.0f - S.tw, S.tw, c->stream));
+    }
+    const float one[4] = {1, 1, 1, 1};
+    const float *dfac = defoFactor ? defoFactor : one;
+    const float4 df = make_float4(dfac[0] * defoAniFac, dfac[1] * defoAniFac,
+                                  dfac[2] * defoAniFac, dfac[3] * defoAniFac);
+    KLP(c, KC_LOOKUP, dst->dims[0], dst->cells() * 8,
+        launch_lookup_slice(dst->f(), dst->dims[0], dst->dims[1], dst->dims[2], phi->f(),
+                            phi->D(), time + overrideTimeOff, blendAlpha, vt.v(),
+                            shape.dims[0], shape.dims[1], shape.dims[2],
+                            make_float4(S.sf[0], S.sf[1], S.sf[2], 0.f),
+                            make_float4(S.off2[0], S.off2[1], S.off2[2], 0.f), df, 0, c->stream,
+                            1));
+    CK(cudaStreamSynchronize(c->stream));
   });
 }
 

@@ -306,6 +306,24 @@ inline void record_solve(flof_ctx *c, int sx, int iters, float res, int status) 
 // C ABI helpers
 // ---------------------------------------------------------------------------
 
+// Host-only work (file headers): no CUDA error to collect.
+template <class F>
+inline int guarded_host(F &&f) {
+  try {
+    f();
+    return FLOF_OK;
+  } catch (const FlofError &e) {
+    g_last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return FLOF_E_OOM;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return FLOF_E_CUDA;
+  }
+}
+
 template <class F>
 inline int guarded(F &&f) {
   try {
@@ -365,4 +383,17 @@ inline void grid_factor4d(const float s1[4], const float s2in[4], const float op
   }
 }
 
+}  // namespace fh
+
+// ---- .uni files (flof_uni.cu) ----------------------------------------------------
+namespace fh {
+struct UniInfo {
+  int dims[4];  // x, y, z and the t extent (1 for a 3D file)
+  bool is4d;
+  int gridType, elementType, bytesPerElement;
+};
+UniInfo uni_info(const char *name);
+void uni_load(flof_grid *g, const char *name);
+void uni_save(const flof_grid *g, const char *name, bool is4d, int gridType);
+void uni_read_slice(flof_grid *g, const char *name, int t);
 }  // namespace fh

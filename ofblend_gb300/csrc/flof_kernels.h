@@ -70,10 +70,12 @@ void launch_deform_twoway(const float4 *vel, const float4 *velInv,
 // vt = (0 + f1*v1) + f2*v2 over one defo t-slice of `cells` cells
 void launch_blend_slices(const float4 *v1, const float4 *v2, float4 *vt,
                          long long cells, float f1, float f2, cudaStream_t s);
+// minBnd: the KERNEL bnd of the lookup, 10 for knSemiLagrangeLookupSlice4d_
+// WithVel (OptRun), 1 for knSemiLagrangeLookupSlice4d (loadAdvectTimeSlice).
 void launch_lookup_slice(float *dst, int dx, int dy, int dz, const float *phi,
                          Dims4 pd, float time, float dt, const float4 *vt,
                          int vx, int vy, int vz, float4 sf3, float4 off3,
-                         float4 defoFactor, int bordSkip, cudaStream_t s);
+                         float4 defoFactor, int bordSkip, cudaStream_t s, int minBnd = 10);
 // Both directions of a two-way frame plus the blend of scenes/flof.py
 // :750-755, in one pass.
 void launch_lookup_slice_twoway(float *dst, int dx, int dy, int dz,
@@ -201,5 +203,7 @@ void launch_set_bound_neumann3(float *a, int X, int Y, int Z, int nc, int w, cud
 void launch_place_slice(float *phi, Dims4 d, int slice, const float *src, const int sdims[3],
                         const float sf[3], const float off[3], float wc, cudaStream_t s);
 void launch_rescale_slices(float *phi, Dims4 d, const float *w, cudaStream_t s);
+// a += v over the bnd = 1 box of a 3D grid
+void launch_add_inner3(float *a, int X, int Y, int Z, float v, cudaStream_t s);
 
 }  // namespace flof

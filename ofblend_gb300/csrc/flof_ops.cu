@@ -493,8 +493,8 @@ __global__ void k_lookup_slice(float *__restrict__ dst, int dx, int dy, BoxDecod
 }
 
 static void lookup_box(int dx, int dy, int dz, int bordSkip, int &lo, int &ex,
-                       int &ey, int &ez) {
-  lo = bordSkip > 10 ? bordSkip : 10;
+                       int &ey, int &ez, int minBnd = 10) {
+  lo = bordSkip > minBnd ? bordSkip : minBnd;
   ex = dx - 2 * lo;
   ey = dy - 2 * lo;
   ez = dz - 2 * lo;
@@ -503,9 +503,9 @@ static void lookup_box(int dx, int dy, int dz, int bordSkip, int &lo, int &ex,
 void launch_lookup_slice(float *dst, int dx, int dy, int dz, const float *phi,
                          Dims4 pd, float time, float dt, const float4 *vt,
                          int vx, int vy, int vz, float4 sf3, float4 off3,
-                         float4 defoFactor, int bordSkip, cudaStream_t s) {
+                         float4 defoFactor, int bordSkip, cudaStream_t s, int minBnd) {
   int lo, ex, ey, ez;
-  lookup_box(dx, dy, dz, bordSkip, lo, ex, ey, ez);
+  lookup_box(dx, dy, dz, bordSkip, lo, ex, ey, ez, minBnd);
   if (ex <= 0 || ey <= 0 || ez <= 0) return;
   BoxDecoder bx = make_decoder(ex, ey, ez, lo, lo, lo, 0);
   const long long nbox = (long long)ex * ey * ez;

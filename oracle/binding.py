@@ -97,6 +97,8 @@ class Oracle:
             "setBound3": (None, [P, P, I, P, I]),
             "setBoundNeumann3": (None, [P, P, I, I]),
             "simpleBlurSpecial": (None, [P, P, I, R, I]),
+            "loadPlaceGrid4d": (None, [P, P, P, P, I, P, P, I, I, I, R, P, R, I, R, I, R, R]),
+            "loadAdvectTimeSlice": (None, [P, P, P, P, P, P, R, R, R, P, P, P, P, R, I, R]),
         }
         for name, (res, args) in sig.items():
             fn = self._f(name)
@@ -224,6 +226,41 @@ class Oracle:
         nc = 4 if a.ndim == 4 else 1
         self._f("setBoundNeumann3")(self._p(self._dims3(a)), self._p(a), nc, int(w))
         return a
+
+    def loadPlaceGrid4d(self, dims, slices, offset, scale, fileIdxStart=-1, fileIdxEnd=-1,
+                        debugSkipLoad=999999, spread=1.0, overrideSize=-1.0, overrideTimeOff=0.0,
+                        overrideGoodRegion=0, loadTimeScale=1.0, rescaleSdfValues=False,
+                        sdfIsoOff=0.0, repeatStartFrame=0.0, phi=None):
+        """slices: array (nfiles, Z, Y, X), element q = file index fileIdxStart + q.
+        phi (optional) is the grid's previous content, kept where the
+        partial-load region says so."""
+        X, Y, Z, T = dims
+        out = np.zeros((T, Z, Y, X), self.dtype) if phi is None else self._arr(phi).copy()
+        sl = self._arr(slices)
+        nf, sz, sy, sx = sl.shape
+        self._f("loadPlaceGrid4d")(
+            self._p(self._dims(dims)), self._p(out), self._p(self._dims((sx, sy, sz))), self._p(sl), nf,
+            self._p(self._vec(offset)), self._p(self._vec(scale)), int(fileIdxStart), int(fileIdxEnd),
+            int(debugSkipLoad), float(spread), self._p(self._vec(overrideSize)), float(overrideTimeOff),
+            int(overrideGoodRegion), float(loadTimeScale), 1 if rescaleSdfValues else 0, float(sdfIsoOff),
+            float(repeatStartFrame))
+        return out
+
+    def loadAdvectTimeSlice(self, defo, dst, phi, time, blendAlpha, loadTimeScale, defoOffset, defoScale,
+                            defoFactor, overrideSize=-1.0, overrideTimeOff=0.0, zeroVel=False,
+                            defoAniFac=1.0):
+        """dst: (Z, Y, X) array, returned updated inside its bnd = 1 box."""
+        d = self._arr(defo)
+        out = self._arr(dst).copy()
+        p = self._arr(phi)
+        z, y, x = out.shape
+        self._f("loadAdvectTimeSlice")(
+            self._p(self._dims(dims_of(d))), self._p(d), self._p(self._dims((x, y, z))), self._p(out),
+            self._p(self._dims(dims_of(p))), self._p(p), float(time), float(blendAlpha),
+            float(loadTimeScale), self._p(self._vec(defoOffset)), self._p(self._vec(defoScale)),
+            self._p(self._vec(defoFactor)), self._p(self._vec(overrideSize)), float(overrideTimeOff),
+            1 if zeroVel else 0, float(defoAniFac))
+        return out
 
     def simpleBlurSpecial(self, a, iter_=1, thresh=0.0, bord=0):
         a = self._arr(a).copy()

@@ -1553,3 +1553,193 @@ EXPORT void ORC_SYM(simpleBlurSpecial)(const int *dims3, REAL *a, int iter,
   if (cur != a) memcpy(a, cur, (size_t)n * sizeof(REAL));
   free(tmp);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Hi-res 4D assembly (scenes/flof.py :707-723)                              */
+/* ------------------------------------------------------------------------ */
+
+/* interpol<Real> (interpol.h:57-95) on a 3D Real grid. */
+static inline REAL interp3_real(const REAL *data, const int *size, idx_t Zs,
+                                const REAL *pos) {
+  REAL px = pos[0] - 0.5f, py = pos[1] - 0.5f, pz = pos[2] - 0.5f;
+  int xi = trunc_int(px), yi = trunc_int(py), zi = trunc_int(pz);
+  REAL s1 = px - (REAL)xi, s0 = (REAL)(1. - s1);
+  REAL t1 = py - (REAL)yi, t0 = (REAL)(1. - t1);
+  REAL f1 = pz - (REAL)zi, f0 = (REAL)(1. - f1);
+  if (px < 0.) { xi = 0; s0 = 1.0; s1 = 0.0; }
+  if (py < 0.) { yi = 0; t0 = 1.0; t1 = 0.0; }
+  if (pz < 0.) { zi = 0; f0 = 1.0; f1 = 0.0; }
+  if (xi >= size[0] - 1) { xi = size[0] - 2; s0 = 0.0; s1 = 1.0; }
+  if (yi >= size[1] - 1) { yi = size[1] - 2; t0 = 0.0; t1 = 1.0; }
+  if (size[2] > 1) {
+    if (zi >= size[2] - 1) { zi = size[2] - 2; f0 = 0.0; f1 = 1.0; }
+  }
+  const idx_t X = 1, Y = size[0], Z = Zs;
+  const idx_t i = (idx_t)xi + (idx_t)size[0] * yi + Zs * zi;
+  return ((data[i] * t0 + data[i + Y] * t1) * s0 +
+          (data[i + X] * t0 + data[i + X + Y] * t1) * s1) *
+             f0 +
+         ((data[i + Z] * t0 + data[i + Y + Z] * t1) * s0 +
+          (data[i + X + Z] * t0 + data[i + X + Y + Z] * t1) * s1) *
+             f1;
+}
+
+/* loadPlaceGrid4d (optflow4d.cpp:1460-1594) with the 3D slice files held in
+ * memory: slices + q * sdims3[0]*sdims3[1]*sdims3[2] is file index
+ * fileIdxStart + q (q < nfiles).  knLoadPlaceGridIpol (:1443-1450) and
+ * knLoadPlaceGridRescale (:1452-1458) run serially over the bnd = 1 box. */
+EXPORT void ORC_SYM(loadPlaceGrid4d)(
+    const int *dims, REAL *phi, const int *sdims3, const REAL *slices, int nfiles,
+    const REAL *offset, const REAL *scale, int fileIdxStart, int fileIdxEnd,
+    int debugSkipLoad, REAL spread, const REAL *overrideSize, REAL overrideTimeOff,
+    int overrideGoodRegion, REAL loadTimeScale, int rescaleSdfValues,
+    REAL sdfIsoOff, REAL repeatStartFrame) {
+  const dims4 d = mkdims(dims);
+  const idx_t n3 = (idx_t)sdims3[0] * sdims3[1] * sdims3[2];
+  const idx_t Zs = sdims3[2] > 1 ? (idx_t)sdims3[0] * sdims3[1] : 0;
+  REAL v1[4] = {(REAL)sdims3[0], (REAL)sdims3[1], (REAL)sdims3[2], 1};
+  REAL defoSize[4] = {(REAL)d.x, (REAL)d.y, (REAL)d.z, (REAL)d.t};
+  if (overrideSize[0] > 0.)
+    for (int c = 0; c < 4; ++c) defoSize[c] = overrideSize[c];
+  REAL sf[4], off2[4], neg1[4] = {-1, -1, -1, -1};
+  for (int c = 0; c < 4; ++c) off2[c] = offset[c];
+  ORC_SYM(gridFactor4d)(v1, defoSize, neg1, scale, sf, off2);
+  REAL valueScale = 1.;
+  if (rescaleSdfValues) valueScale = (REAL)(1. / sf[0]);
+  REAL *w = (REAL *)xcalloc(d.t, sizeof(REAL));
+  const idx_t sT = (idx_t)d.x * d.y * d.z;
+  if (overrideGoodRegion <= 0) {
+    memset(phi, 0, sizeof(REAL) * (size_t)(sT * d.t));
+  } else if (overrideGoodRegion < d.t) {
+    memset(phi + sT * overrideGoodRegion, 0,
+           sizeof(REAL) * (size_t)(sT * (d.t - overrideGoodRegion)));
+  }
+  if (fileIdxStart < 0) fileIdxStart = 0;
+  if (fileIdxEnd < 0) fileIdxEnd = trunc_int(defoSize[3]);
+  int repeatOff = 0;
+  if (repeatStartFrame > 0)
+    repeatOff = trunc_int_d((double)((REAL)(fileIdxEnd - fileIdxStart) * repeatStartFrame) + 1.0);
+  REAL *tmp = (REAL *)xcalloc(n3, sizeof(REAL));
+  const int endId = fileIdxEnd < debugSkipLoad ? fileIdxEnd : debugSkipLoad;
+  for (int fileid = fileIdxStart - repeatOff; fileid < endId; ++fileid) {
+    const int fileidClamp = fileid > fileIdxStart ? fileid : fileIdxStart;
+    int didLoad = 0;
+    const REAL duration =
+        (REAL)(1. * (double)(defoSize[3] * scale[3] / loadTimeScale) /
+               (double)(REAL)(fileIdxEnd - fileIdxStart));
+    const REAL dstt = offset[3] + overrideTimeOff + duration * (REAL)(fileid - fileIdxStart);
+    const int s0 = trunc_int(dstt - spread * duration) + 0;
+    const int s1 = trunc_int(dstt + spread * duration) + 2;
+    for (int slice = s0; slice < s1; ++slice) {
+      if (slice < overrideGoodRegion || slice >= d.t) continue;
+      const REAL q = R_FABS((REAL)slice - dstt) / (duration * spread);
+      const REAL wc = (REAL)(1. - (double)q);
+      if (wc < VEC_EPS) continue;
+      w[slice] += wc;
+      if (!didLoad) {
+        const int qi = fileidClamp - fileIdxStart;
+        if (qi < 0 || qi >= nfiles) abort(); /* the caller supplies every file */
+        memcpy(tmp, slices + (idx_t)qi * n3, sizeof(REAL) * (size_t)n3);
+        if (rescaleSdfValues && sdfIsoOff != 0.) {
+          const int X = sdims3[0], Y = sdims3[1], Z = sdims3[2];
+          for (int k = Z > 1 ? 1 : 0; k < (Z > 1 ? Z - 1 : 1); ++k)
+            for (int j = 1; j < Y - 1; ++j)
+              for (int i = 1; i < X - 1; ++i)
+                tmp[(idx_t)i + (idx_t)X * j + (idx_t)X * Y * k] += sdfIsoOff;
+          const REAL one = 1.;
+          ORC_SYM(setBound3)(sdims3, tmp, 1, &one, 1);
+        }
+        didLoad = 1;
+      }
+      for (int k = 1; k < d.z - 1; ++k)
+        for (int j = 1; j < d.y - 1; ++j)
+          for (int i = 1; i < d.x - 1; ++i) {
+            REAL p[3];
+            p[0] = (REAL)i * sf[0] + off2[0];
+            p[1] = (REAL)j * sf[1] + off2[1];
+            p[2] = (REAL)k * sf[2] + off2[2];
+            phi[index4(d, i, j, k, slice)] += wc * interp3_real(tmp, sdims3, Zs, p);
+          }
+    }
+  }
+  for (int s = 0; s < d.t; ++s) {
+    if (w[s] < 1e-03) {
+      w[s] = 0.;
+    } else {
+      w[s] = (REAL)(1. / w[s]);
+      w[s] *= valueScale;
+    }
+  }
+  for (int t = 1; t < d.t - 1; ++t) {
+    if (w[t] <= 0.) continue;
+    for (int k = 1; k < d.z - 1; ++k)
+      for (int j = 1; j < d.y - 1; ++j)
+        for (int i = 1; i < d.x - 1; ++i) phi[index4(d, i, j, k, t)] *= w[t];
+  }
+  free(tmp);
+  free(w);
+}
+
+/* loadAdvectTimeSlice (optflow4d.cpp:1671-1760), the non-optimised twin of
+ * loadAdvectTimeSlice_OptRun: the deformation slices t and t+1 (defo, held
+ * in memory) are blended, interpolated to the 3D dst size over its bnd = 1
+ * box (loadAdvReInterpol), and knSemiLagrangeLookupSlice4d (:1622-1629)
+ * looks phi up over the same box.  With a t extent of 1 the reference's
+ * fourd kernel runs its 3D branch at t = 0 (codegen_kernel.cpp:243-263). */
+EXPORT void ORC_SYM(loadAdvectTimeSlice)(
+    const int *defoDims, const REAL *defo, const int *dstDims, REAL *dst,
+    const int *phiDims, const REAL *phi, REAL time, REAL blendAlpha,
+    REAL loadTimeScale, const REAL *defoOffset, const REAL *defoScale,
+    const REAL *defoFactor, const REAL *overrideSize, REAL overrideTimeOff,
+    int zeroVel, REAL defoAniFac) {
+  const int dimT = defoDims[3];
+  REAL dim4[4] = {(REAL)defoDims[0], (REAL)defoDims[1], (REAL)defoDims[2],
+                  (REAL)defoDims[3]};
+  int defoSizeI[4] = {phiDims[0], phiDims[1], phiDims[2], phiDims[3]};
+  if (overrideSize[0] > 0.)
+    for (int c = 0; c < 4; ++c) defoSizeI[c] = trunc_int(overrideSize[c]);
+  REAL defoSize[4], sf[4], off2[4], neg1[4] = {-1, -1, -1, -1};
+  for (int c = 0; c < 4; ++c) {
+    defoSize[c] = (REAL)defoSizeI[c];
+    off2[c] = defoOffset[c];
+  }
+  ORC_SYM(gridFactor4d)(dim4, defoSize, neg1, defoScale, sf, off2);
+  REAL srcTime = (REAL)((double)(time * sf[3] * loadTimeScale + off2[3]) - 0.5);
+  int t = trunc_int(srcTime);
+  int tp1 = t + 1;
+  REAL tw = srcTime - (REAL)t;
+  if (t > dimT - 1) t = dimT - 1;
+  if (tp1 > dimT - 1) tp1 = dimT - 1;
+  const idx_t slice = (idx_t)defoDims[0] * defoDims[1] * defoDims[2];
+  REAL *v1 = (REAL *)xcalloc(slice * 4, sizeof(REAL));
+  const REAL *a = defo + (idx_t)t * slice * 4;
+  const REAL *b = defo + (idx_t)tp1 * slice * 4;
+  const REAL f1 = (REAL)(1. - tw), f2 = tw;
+  /* v1.multConst(1-tw); v2.multConst(tw); v1.add(v2) */
+  for (idx_t q = 0; q < slice * 4; ++q) v1[q] = a[q] * f1 + b[q] * f2;
+  if (zeroVel)
+    for (idx_t q = 0; q < slice * 4; ++q) v1[q] = 0.;
+  const int X = dstDims[0], Y = dstDims[1], Z = dstDims[2];
+  const idx_t vZ = (idx_t)defoDims[0] * defoDims[1];
+  REAL df[4];
+  for (int c = 0; c < 4; ++c) df[c] = defoFactor[c] * defoAniFac;
+  const dims4 pd = mkdims(phiDims);
+  const REAL T0 = time + overrideTimeOff;
+  for (int k = 1; k < Z - 1; ++k)
+    for (int j = 1; j < Y - 1; ++j)
+      for (int i = 1; i < X - 1; ++i) {
+        REAL pos3[3];
+        pos3[0] = (REAL)i * sf[0] + off2[0];
+        pos3[1] = (REAL)j * sf[1] + off2[1];
+        pos3[2] = (REAL)k * sf[2] + off2[2];
+        vec4 v = interp3_vec4(v1, defoDims, vZ, pos3);
+        for (int c = 0; c < 4; ++c) v.v[c] *= df[c];
+        REAL pos4[4];
+        pos4[0] = (REAL)(i + 0.5f) - v.v[0] * blendAlpha;
+        pos4[1] = (REAL)(j + 0.5f) - v.v[1] * blendAlpha;
+        pos4[2] = (REAL)(k + 0.5f) - v.v[2] * blendAlpha;
+        pos4[3] = (REAL)(T0 + 0.5f) - v.v[3] * blendAlpha;
+        dst[(idx_t)i + (idx_t)X * j + (idx_t)X * Y * k] = interp4_real(phi, pd, pos4);
+      }
+  free(v1);
+}
