@@ -24,6 +24,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <type_traits>
+
 #include "flof_kernels.h"
 
 namespace flof {
@@ -31,26 +33,27 @@ namespace flof {
 namespace {
 
 constexpr int TX = 32;                // tile width: one column per lane
-constexpr int NWARP = 4;
-constexpr int NTHR = TX * NWARP;      // 128
 constexpr int WAIT_LIMIT = 1 << 22;   // try_wait polls before giving up
 
-// Tile geometry: RY rows per thread, DT consecutive t planes per block,
-// NSTAGE slab buffers in flight.
-template <int S, int RY_, int DT_, int NSTAGE_>
+// Tile geometry: NW warps, RY rows per thread, DT consecutive t planes and DZ
+// consecutive z planes per block, NSTAGE slab buffers in flight.
+template <int S, int NW_, int RY_, int DT_, int DZ_, int NSTAGE_, int MINB_ = 1>
 struct TG {
-  static constexpr int RY = RY_, DT = DT_, NSTAGE = NSTAGE_;
-  static constexpr int TY = NWARP * RY;
+  static constexpr int NW = NW_, RY = RY_, DT = DT_, DZ = DZ_, NSTAGE = NSTAGE_, MINB = MINB_;
+  static constexpr int NTHR = 32 * NW;
+  static constexpr int TY = NW * RY;
   static constexpr int W = TX + 2 * S, H = TY + 2 * S, N = W * H;
   static constexpr int BYTES = N * 16;                   // one slab
   static constexpr int STRIDE = (BYTES + 127) / 128 * 128;  // slab start spacing
   static constexpr int SMEM = NSTAGE * STRIDE;
+  static_assert(DZ * DT * RY <= 16, "the keep mask holds 16 cells per thread");
 };
-// The blur (S = 1, 2) is bound by its multiply-adds: one t plane, 32 rows.
-// The extrapolation sweep has one add per tap and is bound by how fast slabs
-// reach shared memory: four t planes share every slab, four slabs in flight.
-template <int S> using BlurGeom = TG<S, 8, 1, 2>;
-using ExpolGeom = TG<1, 4, 4, 4>;
+// The blur (S = 1, 2) is bound by its multiply-adds: one (z, t) plane per
+// block, 32 rows.  The extrapolation sweep has one add per tap and is bound by
+// how fast slabs reach shared memory and registers: four t planes and two z
+// planes share every slab (24 slabs per 8 output planes), four in flight.
+template <int S> using BlurGeom = TG<S, 4, 8, 1, 1, 2>;
+using ExpolGeom = TG<1, 8, 2, 4, 2, 4, 3>;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -87,17 +90,35 @@ __device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map,
       : "memory");
 }
 
+// The extrapolation sweep adds with sm_100-family packed `add.rn.f32x2`: a
+// float4 is two float pairs (x,y), (z,w), each lane rounded like the scalar
+// add, so the sums are bit for bit the scalar ones in the same order at half
+// the instruction count (4M random pairs on GB300: no difference).  The blur
+// keeps scalar multiplies and adds: a packed multiply followed by a packed add
+// gave results different from the scalar multiply-then-add in about 15% of
+// 4M random cases on GB300, which would break the reference's two roundings.
+struct __align__(16) P4 {
+  unsigned long long lo, hi;
+};
+__device__ __forceinline__ void add2(unsigned long long &acc, unsigned long long x) {
+  asm("add.rn.f32x2 %0, %0, %1;" : "+l"(acc) : "l"(x));
+}
+__device__ __forceinline__ void acc4(P4 &v, const P4 &a) {
+  add2(v.lo, a.lo);
+  add2(v.hi, a.hi);
+}
+__device__ __forceinline__ float4 unpack4(const P4 &v) {
+  float4 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v.lo));
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.z), "=f"(r.w) : "l"(v.hi));
+  return r;
+}
+__device__ __forceinline__ float4 unpack4(const float4 &v) { return v; }
 __device__ __forceinline__ void mac4(float4 &v, float w, const float4 &a) {
   v.x += w * a.x;
   v.y += w * a.y;
   v.z += w * a.z;
   v.w += w * a.w;
-}
-__device__ __forceinline__ void acc4(float4 &v, const float4 &a) {
-  v.x += a.x;
-  v.y += a.y;
-  v.z += a.z;
-  v.w += a.w;
 }
 
 template <int S>
@@ -116,33 +137,35 @@ struct WTabT {
 };
 
 // MODE 0: Gaussian blur pass; MODE 1: extrapolation sweep.  A block computes
-// the outputs of DT consecutive t planes at one z.  It walks the input slabs
+// the outputs of DZ x DT consecutive (z, t) planes.  It walks the input slabs
 // (tt, zz) of the union of their neighbourhoods in lexicographic order; for a
-// fixed output plane t_o that order is the reference's (vt, zk) order with
-// vt = tt - t_o, zk = zz - z, so every output still adds its taps in the
-// reference's sequence while each slab is fetched once for all DT planes.
+// fixed output plane (z_o, t_o) that order is the reference's (vt, zk) order
+// with vt = tt - t_o, zk = zz - z_o, so every output still adds its taps in
+// the reference's sequence while each slab is fetched once for all planes.
 template <int S, int MODE, class G>
-__global__ void __launch_bounds__(NTHR)
+__global__ void __launch_bounds__(G::NTHR, G::MINB)
 k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
            int tiles_x, const float *__restrict__ wsum, const uint16_t *__restrict__ fixed,
            WTabT wt, int zero_border, int *err) {
-  constexpr int RY = G::RY, DT = G::DT, NS = G::NSTAGE;
+  constexpr int RY = G::RY, DT = G::DT, DZ = G::DZ, NS = G::NSTAGE;
   extern __shared__ __align__(128) unsigned char raw[];
   __shared__ __align__(8) uint64_t bar[NS];
   __shared__ float wsh[40];
 
   const int tile = blockIdx.x;
   const int x0 = (tile % tiles_x) * TX, y0 = (tile / tiles_x) * G::TY;
-  const int z = blockIdx.y, t0 = blockIdx.z * DT;
+  const int z0 = blockIdx.y * DZ, t0 = blockIdx.z * DT;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int x = x0 + tx;
-  const int ygroups = (d.y + RY - 1) / RY;
-  const int yg = y0 / RY + ty;
-  // MODE 1: bit o*RY+q set = cell (x, y0+RY*ty+q, z, t0+o) keeps its value
-  // (loaded now, used after the slab walk)
+  // MODE 1: bit (oz*DT + o)*RY + q set = cell (x, y0+RY*ty+q, z0+oz, t0+o)
+  // keeps its value (loaded now, used after the slab walk)
   unsigned keep = 0xffffu;
-  if (MODE == 1 && x < d.x && yg < ygroups)
-    keep = __ldg(fixed + (((size_t)blockIdx.z * d.z + z) * ygroups + yg) * d.x + x);
+  if (MODE == 1) {
+    const int ygroups = (d.y + RY - 1) / RY, zgroups = (d.z + DZ - 1) / DZ;
+    const int yg = y0 / RY + ty;
+    if (x < d.x && yg < ygroups)
+      keep = __ldg(fixed + (((size_t)blockIdx.z * zgroups + blockIdx.y) * ygroups + yg) * d.x + x);
+  }
 
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -152,14 +175,14 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   if (MODE == 0 && threadIdx.x < 40) wsh[threadIdx.x] = wt.w[threadIdx.x];
   __syncthreads();
 
-  constexpr int K = 2 * S + 1;
-  constexpr int NP = (DT + 2 * S) * K;  // slabs (tt, zz), tt-major
+  constexpr int KZ = DZ + 2 * S;
+  constexpr int NP = (DT + 2 * S) * KZ;  // slabs (tt, zz), tt-major
   // slab p lives in buffer p % NS; its barrier completes phase (p / NS) & 1
   auto issue = [&](int p) {
     uint64_t *b = &bar[p % NS];
     mbar_expect_tx(b, G::BYTES);
-    tma_load_slab(raw + (p % NS) * G::STRIDE, &map, x0 - S, y0 - S, z + (p % K - S),
-                  t0 - S + p / K, b);
+    tma_load_slab(raw + (p % NS) * G::STRIDE, &map, x0 - S, y0 - S, z0 - S + p % KZ,
+                  t0 - S + p / KZ, b);
   };
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -167,14 +190,18 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       if (p < NP) issue(p);
   }
 
-  float4 val[DT][RY];
+  // accumulator / slab element: float4 for the blur, packed pairs for the sweep
+  typedef typename std::conditional<MODE == 0, float4, P4>::type V4;
+  V4 val[DZ][DT][RY];
 #pragma unroll
-  for (int o = 0; o < DT; ++o)
+  for (int oz = 0; oz < DZ; ++oz)
 #pragma unroll
-    for (int q = 0; q < RY; ++q) val[o][q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int o = 0; o < DT; ++o)
+#pragma unroll
+      for (int q = 0; q < RY; ++q) memset(&val[oz][o][q], 0, sizeof(V4));
 
   for (int p = 0; p < NP; ++p) {
-    const int tt = t0 - S + p / K, zk = p % K - S;
+    const int vt0 = p / KZ - S, zk0 = p % KZ - S;  // offsets seen by plane (0, 0)
     // buffer (p - 1) % NS was released by the barrier that ended step p - 1
     if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
     const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
@@ -187,32 +214,38 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       __syncthreads();
       return;
     }
-    const float4 *cur = (const float4 *)(raw + (p % NS) * G::STRIDE);
+    const V4 *cur = (const V4 *)(raw + (p % NS) * G::STRIDE);
     // slab rows RY*ty .. RY*ty+RY-1+2S feed output rows RY*ty+q via yj = k-q-S
 #pragma unroll
     for (int k = 0; k < RY + 2 * S; ++k) {
-      const float4 *row = cur + (RY * ty + k) * G::W + tx;
-      float4 a[2 * S + 1];
+      const V4 *row = cur + (RY * ty + k) * G::W + tx;
+      V4 a[2 * S + 1];
 #pragma unroll
       for (int m = 0; m <= 2 * S; ++m) a[m] = row[m];
 #pragma unroll
-      for (int o = 0; o < DT; ++o) {
-        const int vt = tt - (t0 + o);
-        if (vt < -S || vt > S) continue;
+      for (int oz = 0; oz < DZ; ++oz) {
+        const int zk = zk0 - oz;
+        if (zk < -S || zk > S) continue;
 #pragma unroll
-        for (int q = 0; q < RY; ++q) {
-          const int yj = k - q - S;
-          if (yj < -S || yj > S) continue;
-          if (MODE == 0) {
-            const int base = vt * vt + zk * zk + yj * yj;
-            float wx[S + 1];
+        for (int o = 0; o < DT; ++o) {
+          const int vt = vt0 - o;
+          if (vt < -S || vt > S) continue;
 #pragma unroll
-            for (int e = 0; e <= S; ++e) wx[e] = wsh[base + e * e];
+          for (int q = 0; q < RY; ++q) {
+            const int yj = k - q - S;
+            if (yj < -S || yj > S) continue;
+            if constexpr (MODE == 0) {
+              const int base = vt * vt + zk * zk + yj * yj;
+              float wx[S + 1];
 #pragma unroll
-            for (int xi = -S; xi <= S; ++xi) mac4(val[o][q], wx[xi < 0 ? -xi : xi], a[xi + S]);
-          } else {
+              for (int e = 0; e <= S; ++e) wx[e] = wsh[base + e * e];
 #pragma unroll
-            for (int xi = -S; xi <= S; ++xi) acc4(val[o][q], a[xi + S]);
+              for (int xi = -S; xi <= S; ++xi)
+                mac4(val[oz][o][q], wx[xi < 0 ? -xi : xi], a[xi + S]);
+            } else {
+#pragma unroll
+              for (int xi = -S; xi <= S; ++xi) acc4(val[oz][o][q], a[xi + S]);
+            }
           }
         }
       }
@@ -223,29 +256,34 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   if (x >= d.x) return;
   constexpr int P1 = (S + 1) * (S + 1);
 #pragma unroll
-  for (int o = 0; o < DT; ++o) {
-    const int t = t0 + o;
-    if (t >= d.t) break;
-    const bool zt_inner = z >= 1 && z < d.z - 1 && t >= 1 && t < d.t - 1;
-    const int code_zt =
-        MODE == 0 ? ((clip_code_t<S>(t, d.t) * P1 + clip_code_t<S>(z, d.z)) * P1) : 0;
+  for (int oz = 0; oz < DZ; ++oz) {
+    const int z = z0 + oz;
+    if (z >= d.z) break;
 #pragma unroll
-    for (int q = 0; q < RY; ++q) {
-      const int y = y0 + RY * ty + q;
-      if (y >= d.y) continue;
-      const idx_t id = d.index(x, y, z, t);
-      const float4 v = val[o][q];
-      if (MODE == 0) {
-        if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
-          if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
-          continue;
+    for (int o = 0; o < DT; ++o) {
+      const int t = t0 + o;
+      if (t >= d.t) break;
+      const bool zt_inner = z >= 1 && z < d.z - 1 && t >= 1 && t < d.t - 1;
+      const int code_zt =
+          MODE == 0 ? ((clip_code_t<S>(t, d.t) * P1 + clip_code_t<S>(z, d.z)) * P1) : 0;
+#pragma unroll
+      for (int q = 0; q < RY; ++q) {
+        const int y = y0 + RY * ty + q;
+        if (y >= d.y) continue;
+        const idx_t id = d.index(x, y, z, t);
+        const float4 v = unpack4(val[oz][o][q]);
+        if (MODE == 0) {
+          if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
+            if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+            continue;
+          }
+          const float ws =
+              __ldg(wsum + (code_zt + clip_code_t<S>(y, d.y)) * P1 + clip_code_t<S>(x, d.x));
+          dst[id] = make_float4(v.x / ws, v.y / ws, v.z / ws, v.w / ws);
+        } else {
+          if (keep >> ((oz * DT + o) * RY + q) & 1u) continue;
+          dst[id] = make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
         }
-        const float ws =
-            __ldg(wsum + (code_zt + clip_code_t<S>(y, d.y)) * P1 + clip_code_t<S>(x, d.x));
-        dst[id] = make_float4(v.x / ws, v.y / ws, v.z / ws, v.w / ws);
-      } else {
-        if (keep >> (o * RY + q) & 1u) continue;
-        dst[id] = make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
       }
     }
   }
@@ -290,12 +328,12 @@ template <int S, int MODE, class G>
 bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
                 const uint16_t *fixed, const float *w, int zero_border, int *err,
                 cudaStream_t st) {
-  const int tgroups = (d.t + G::DT - 1) / G::DT;
-  if (d.z > 65535 || tgroups > 65535) return false;
+  const int tgroups = (d.t + G::DT - 1) / G::DT, zgroups = (d.z + G::DZ - 1) / G::DZ;
+  if (zgroups > 65535 || tgroups > 65535) return false;
   CUtensorMap map;
   if (!encode_slab_map(&map, src, d, G::W, G::H)) return false;
   const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + G::TY - 1) / G::TY;
-  dim3 grid(tiles_x * tiles_y, d.z, tgroups);
+  dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
   const size_t smem = G::SMEM;
   static bool attr = false;
   if (!attr) {
@@ -308,8 +346,8 @@ bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
   }
   WTabT wt;
   for (int i = 0; i < 40; ++i) wt.w[i] = (w && i <= 4 * S * S) ? w[i] : 0.f;
-  k_slab_tma<S, MODE, G><<<grid, NTHR, smem, st>>>(map, dst, d, tiles_x, wsum, fixed, wt,
-                                                  zero_border, err);
+  k_slab_tma<S, MODE, G><<<grid, G::NTHR, smem, st>>>(map, dst, d, tiles_x, wsum, fixed, wt,
+                                                     zero_border, err);
   return true;
 }
 
@@ -328,29 +366,31 @@ bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const floa
 
 namespace {
 
-// One 16-bit word per sweep thread: (x, y group of RY rows, z, t group of DT
-// planes), x fastest.  A bit is set for each cell of the thread's RY x DT
-// outputs that the sweep leaves alone: marked, outside the interior
-// (knCvExpolBlur4d runs over bnd = 1), or past the grid's end.
+// One 16-bit word per sweep thread: (x, y group of RY rows, z group of DZ, t
+// group of DT), x fastest.  A bit is set for each of the thread's cells that
+// the sweep leaves alone: marked, outside the interior (knCvExpolBlur4d runs
+// over bnd = 1), or past the grid's end.
 __global__ void k_expol_mask(const float *__restrict__ mark, uint16_t *__restrict__ mask,
-                             Dims4 d, int ygroups, long long nwords) {
-  constexpr int RY = ExpolGeom::RY, DT = ExpolGeom::DT;
+                             Dims4 d, int ygroups, int zgroups, long long nwords) {
+  constexpr int RY = ExpolGeom::RY, DT = ExpolGeom::DT, DZ = ExpolGeom::DZ;
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nwords;
        w += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(w % d.x);
     long long r = w / d.x;
     const int yg = (int)(r % ygroups);
     r /= ygroups;
-    const int z = (int)(r % d.z);
-    const int tg = (int)(r / d.z);
+    const int zg = (int)(r % zgroups);
+    const int tg = (int)(r / zgroups);
     unsigned bits = 0;
-    for (int o = 0; o < DT; ++o)
-      for (int q = 0; q < RY; ++q) {
-        const int y = yg * RY + q, t = tg * DT + o;
-        const bool inner = x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1 && z >= 1 &&
-                           z < d.z - 1 && t >= 1 && t < d.t - 1;
-        if (!inner || __ldg(mark + d.index(x, y, z, t)) != 0.f) bits |= 1u << (o * RY + q);
-      }
+    for (int oz = 0; oz < DZ; ++oz)
+      for (int o = 0; o < DT; ++o)
+        for (int q = 0; q < RY; ++q) {
+          const int y = yg * RY + q, z = zg * DZ + oz, t = tg * DT + o;
+          const bool inner = x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1 && z >= 1 &&
+                             z < d.z - 1 && t >= 1 && t < d.t - 1;
+          if (!inner || __ldg(mark + d.index(x, y, z, t)) != 0.f)
+            bits |= 1u << ((oz * DT + o) * RY + q);
+        }
     mask[w] = (uint16_t)bits;
   }
 }
@@ -358,14 +398,15 @@ __global__ void k_expol_mask(const float *__restrict__ mark, uint16_t *__restric
 }  // namespace
 
 size_t expol_mask_words(Dims4 d) {
-  return (size_t)d.x * ((d.y + ExpolGeom::RY - 1) / ExpolGeom::RY) * d.z *
-         ((d.t + ExpolGeom::DT - 1) / ExpolGeom::DT);
+  return (size_t)d.x * ((d.y + ExpolGeom::RY - 1) / ExpolGeom::RY) *
+         ((d.z + ExpolGeom::DZ - 1) / ExpolGeom::DZ) * ((d.t + ExpolGeom::DT - 1) / ExpolGeom::DT);
 }
 
 void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st) {
   const long long n = (long long)expol_mask_words(d);
   const int ygroups = (d.y + ExpolGeom::RY - 1) / ExpolGeom::RY;
-  k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, mask, d, ygroups, n);
+  const int zgroups = (d.z + ExpolGeom::DZ - 1) / ExpolGeom::DZ;
+  k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, mask, d, ygroups, zgroups, n);
 }
 
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
