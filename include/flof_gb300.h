@@ -132,10 +132,14 @@ FLOF_API const char *flof_kernel_class_name(int cls);
  * FLOF_OPT_CFL_SYNC: 0 (default) the CFL substep count of advectCflHelper4d
  *   (optflow4d.cpp:1309-1321) is checked on the device and a call that needs
  *   more than one substep is redone; 1 the host reads max |v| before every
- *   CFL-guarded advection. */
-enum { FLOF_OPT_CFL_SYNC = 2 };
+ *   CFL-guarded advection.
+ * FLOF_OPT_AUTOTUNE: 1 times a few launch shapes of the PCG kernels once per
+ *   grid size and keeps the fastest; 0 (default) uses fixed shapes.  Shapes
+ *   group the dot-product partial sums differently, so tuned and untuned runs
+ *   agree to rounding, not bit for bit. */
+enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3 };
 FLOF_API int flof_ctx_set_option(flof_ctx *ctx, int option, int value);
-/* Release cached device buffers of the context's pool. */
+/* Release cached device buffers of the context's pool (and its workers'). */
 FLOF_API int flof_ctx_trim(flof_ctx *ctx);
 
 /* ---- grids: Grid4d<Real>, Grid4d<Vec4> (source/grid4d.h:117-265) -------- */
@@ -185,6 +189,19 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *ctx, flof_grid *vel,
                                           const flof_grid *i1,
                                           const flof_of_params *params,
                                           float *err, flof_solve_stats *stats);
+
+/* Batched opticalFlowMultiscale4d: n independent solves with the same
+ * parameters and any grid sizes (vels[q], i0s[q], i1s[q] of one size per q).
+ * They run concurrently on `workers` worker streams of the context, each
+ * driven by its own host thread; workers <= 0 picks the count from the
+ * sizes.  Every solve gives the same result as the single call on the same
+ * grids.  errs (nullable) receives n error metrics. */
+FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *ctx, int n,
+                                                flof_grid *const *vels,
+                                                const flof_grid *const *i0s,
+                                                const flof_grid *const *i1s,
+                                                const flof_of_params *params,
+                                                float *errs, int workers);
 
 /* opticalFlow4d (optflow4d.cpp:2110-2119 -> opticalFlowDim :361-553): one
  * level, one solve.  iterations / residual (nullable) report the PCG. */

@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(_HERE, "libflof_gb300.so")
 FLOF_REAL = 1
 FLOF_VEC4 = 8
 FLOF_OPT_CFL_SYNC = 2
+FLOF_OPT_AUTOTUNE = 3
 MAX_SOLVE_STATS = 64
 
 STATUS = {
@@ -142,6 +143,7 @@ SIGNATURES = {
     "flof_uni_read_slice": (I, [P, ctypes.c_char_p, I]),
     "flof_loadAdvectTimeSlice_OptInitFile": (I, [P, I, ctypes.c_char_p, I, I, F]),
     "flof_loadAdvectTimeSlice": (I, [P, P, ctypes.c_char_p, P, P, F, F, F, P, P, P, P, F, I, F]),
+    "flof_opticalFlowMultiscale4d_batch": (I, [P, I, P, P, P, P, FP, I]),
 }
 
 _lib = None

@@ -35,6 +35,7 @@ __all__ = [
     "loadAdvectTimeSlice_OptRunTwoway", "loadAdvectTimeSlice_Finish", "last_solve_stats",
     "LevelsetGrid", "repeatFrame4d", "extrap4dLsSimple", "simpleBlurSpecial", "shiftForwGrid4d",
     "uniFileInfo", "getUniFileSize", "readGrid4dUniSlice", "loadPlaceGrid4d", "loadAdvectTimeSlice",
+    "opticalFlowMultiscale4d_batch",
 ]
 
 
@@ -363,13 +364,9 @@ def _ctx_of(g) -> Context:
     return g.ctx
 
 
-def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
-                            cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
-                            resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
-                            doFinalProject=False, cgMaxIter=1000):
-    """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
-    error metric (the reference's template returns it to C++ callers)."""
-    global _last_stats
+def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e-04, blurType=1, cfl=999,
+               orderTime=1, orderSpace=1, resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999,
+               minGridSize=10, doFinalProject=False, cgMaxIter=1000):
     p = OFParams()
     _lib.lib().flof_of_params_default(ctypes.byref(p))
     p.wSmooth, p.wEnergy, p.level = wSmooth, wEnergy, int(level)
@@ -378,6 +375,18 @@ def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, le
     p.resetBndWidth, p.multiStep = resetBndWidth, int(multiStep)
     p.projSizeThresh, p.minGridSize = int(projSizeThresh), int(minGridSize)
     p.doFinalProject, p.cgMaxIter = int(bool(doFinalProject)), int(cgMaxIter)
+    return p
+
+
+def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
+                            cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
+                            resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
+                            doFinalProject=False, cgMaxIter=1000):
+    """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
+    error metric (the reference's template returns it to C++ callers)."""
+    global _last_stats
+    p = _of_params(wSmooth, wEnergy, level, postVelBlur, cgAccuracy, blurType, cfl, orderTime, orderSpace,
+                   resetBndWidth, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter)
     err = ctypes.c_float()
     st = SolveStats()
     ctx = _ctx_of(vel)
@@ -385,6 +394,24 @@ def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, le
                                                ctypes.byref(err), ctypes.byref(st)))
     _last_stats = st.as_dict()
     return float(err.value)
+
+
+def opticalFlowMultiscale4d_batch(vels, i0s, i1s, workers=0, **params):
+    """Independent opticalFlowMultiscale4d solves (same keyword parameters,
+    any sizes) run concurrently on worker streams; returns the error metrics.
+    Each result equals the single call's on the same grids."""
+    n = len(vels)
+    if not (len(i0s) == n and len(i1s) == n):
+        raise FlofError(1, "vels, i0s and i1s must have the same length")
+    if n == 0:
+        return []
+    p = _of_params(**params)
+    ctx = _ctx_of(vels[0])
+    arr = lambda gs: (ctypes.c_void_p * n)(*[g.h.value for g in gs])
+    errs = (ctypes.c_float * n)()
+    check(ctx.lib.flof_opticalFlowMultiscale4d_batch(ctx.h, n, arr(vels), arr(i0s), arr(i1s), ctypes.byref(p),
+                                                     errs, int(workers)))
+    return [float(e) for e in errs]
 
 
 def opticalFlow4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, postVelBlur=0.0, cgAccuracy=1e-04,

@@ -1,0 +1,128 @@
+// flof_batch.cu -- many independent deformation solves of uneven grid sizes
+// on one GPU.  A solve at 24^3 x 16 cells launches kernels of a few
+// microseconds, far too small to fill 152 SMs, and spends much of its time
+// in host round trips (CG convergence checks, multistep decisions).  The
+// batch runs the solves concurrently: each worker context owns a CUDA stream,
+// a buffer pool and the PCG state, and one host thread drives it through the
+// same multiscale driver as the single call, so kernels of different solves
+// overlap on the GPU and one solve's host round trip hides behind another's
+// kernels.  Solves are handed out largest first from a shared counter.
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <thread>
+
+#include "flof_internal.h"
+
+using namespace flof;
+using namespace fh;
+
+namespace {
+
+flof_ctx *worker(flof_ctx *c, size_t q) {
+  while (c->workers.size() <= q) {
+    flof_ctx *w = nullptr;
+    if (flof_ctx_create(c->device, &w) != FLOF_OK) fail(FLOF_E_CUDA, g_last_error);
+    w->cfl_force_sync = c->cfl_force_sync;
+    w->autotune = c->autotune;
+    w->tune_owner = c;
+    c->workers.push_back(w);
+  }
+  return c->workers[q];
+}
+
+// Worker count when the caller leaves it open: enough streams that about
+// 64M cells of the largest solve are in flight (one 64^4 solve alone keeps
+// the PCG kernels near the HBM roofline), at most 16 and at most one per
+// solve.
+int auto_workers(const std::vector<long long> &cells) {
+  long long total = 0, big = 0;
+  for (long long n : cells) {
+    total += n;
+    big = n > big ? n : big;
+  }
+  int w = (int)((64ll << 20) / (big > 0 ? big : 1));
+  if (w < 1) w = 1;
+  if (w > 16) w = 16;
+  if (w > (int)cells.size()) w = (int)cells.size();
+  return w;
+}
+
+}  // namespace
+
+FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *c, int n, flof_grid *const *vels,
+                                                const flof_grid *const *i0s,
+                                                const flof_grid *const *i1s,
+                                                const flof_of_params *params, float *errs,
+                                                int workers) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need(n >= 0, "n must not be negative");
+    if (n == 0) return;
+    need(vels != nullptr && i0s != nullptr && i1s != nullptr, "NULL grid list");
+    std::vector<long long> cells(n);
+    for (int q = 0; q < n; ++q) {
+      need_grid(vels[q], "vel");
+      need_grid(i0s[q], "i0");
+      need_grid(i1s[q], "i1");
+      need_elem(vels[q], FLOF_VEC4, "vel");
+      need_elem(i0s[q], FLOF_REAL, "i0");
+      need_elem(i1s[q], FLOF_REAL, "i1");
+      same_size(vels[q], i0s[q], "opticalFlowMultiscale4d_batch");
+      same_size(vels[q], i1s[q], "opticalFlowMultiscale4d_batch");
+      need_4d(vels[q], "vel");
+      cells[q] = vels[q]->cells();
+    }
+    set_ctx_device(c);
+    int nw = workers > 0 ? workers : auto_workers(cells);
+    if (nw > n) nw = n;
+    // largest first
+    std::vector<int> order(n);
+    for (int q = 0; q < n; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return cells[a] > cells[b]; });
+    // the inputs may still be in flight on the caller's stream
+    cudaEvent_t ready;
+    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(ready, c->stream));
+    std::vector<flof_ctx *> ws(nw);
+    for (int q = 0; q < nw; ++q) {
+      ws[q] = worker(c, q);
+      CK(cudaStreamWaitEvent(ws[q]->stream, ready, 0));
+    }
+    CK(cudaEventDestroy(ready));
+
+    std::atomic<int> next(0);
+    std::mutex mu;
+    int first_status = FLOF_OK;
+    std::string first_msg;
+    auto run = [&](flof_ctx *w) {
+      cudaSetDevice(w->device);
+      for (;;) {
+        const int k = next.fetch_add(1);
+        if (k >= n) break;
+        const int q = order[k];
+        float e = 0.f;
+        const int st = flof_opticalFlowMultiscale4d(w, vels[q], i0s[q], i1s[q], params, &e,
+                                                    nullptr);
+        if (st != FLOF_OK) {
+          std::lock_guard<std::mutex> lk(mu);
+          if (first_status == FLOF_OK) {
+            first_status = st;
+            first_msg = "solve " + std::to_string(q) + ": " + g_last_error;
+          }
+          next.store(n);  // stop handing out work
+          break;
+        }
+        if (errs) errs[q] = e;
+      }
+    };
+    std::vector<std::thread> threads;
+    threads.reserve(nw > 0 ? nw - 1 : 0);
+    for (int q = 1; q < nw; ++q) threads.emplace_back(run, ws[q]);
+    run(ws[0]);
+    for (auto &t : threads) t.join();
+    for (flof_ctx *w : ws) CK(cudaStreamSynchronize(w->stream));
+    if (first_status != FLOF_OK) fail(first_status, first_msg);
+  });
+}

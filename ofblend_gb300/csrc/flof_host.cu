@@ -190,6 +190,79 @@ struct OFArgs {
 // opticalFlowDim<Grid4d<Real>,Grid4d<Vec4>,4> (optflow4d.cpp:361-553).
 // velIn (nullable) is the input velocity used in the rhs; the result goes
 // to velOut (may alias velIn).
+// PCG launch shapes for grid size d: the defaults, or (FLOF_OPT_AUTOTUNE)
+// the fastest of a few candidates timed once per size on scratch buffers.
+// The candidates give the same per-cell arithmetic; the grouping of the dot
+// product partial sums, and so the last bits of alpha and beta, differ.
+CGTune cg_tune(flof_ctx *c, Dims4 d, const OFConsts &k) {
+  CGTune best;
+  if (!c->autotune || d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3) return best;
+  const std::array<int, 4> key = {d.x, d.y, d.z, d.t};
+  flof_ctx *owner = c->tune_owner ? c->tune_owner : c;
+  std::lock_guard<std::mutex> lock(owner->tune_mu);
+  auto it = owner->tunes.find(key);
+  if (it != owner->tunes.end()) return it->second;
+  const size_t vb = vec_bytes(d);
+  DBuf p(c, vb), g(c, vb), q(c, vb), x(c, vb), r(c, vb), stb(c, sizeof(CGState));
+  CK(cudaMemsetAsync(p.p, 0, vb, c->stream));
+  CK(cudaMemsetAsync(g.p, 0, vb, c->stream));
+  CK(cudaMemsetAsync(x.p, 0, vb, c->stream));
+  CK(cudaMemsetAsync(r.p, 0, vb, c->stream));
+  // a private PCG state that never converges (acc < 0) and never divides by 0
+  CGState init;
+  memset(&init, 0, sizeof(init));
+  init.sigma = 1.0;
+  init.acc = -1.0;
+  init.resIni = 1.0;
+  CK(cudaMemcpyAsync(stb.p, &init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
+  CGState *st = (CGState *)stb.p;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto time_it = [&](auto &&launch) {
+    launch();  // warm-up
+    CK(cudaEventRecord(e0, c->stream));
+    for (int rep = 0; rep < 3; ++rep) launch();
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    return ms;
+  };
+  float bt = 1e30f;
+  for (int tt : {4, 8, 16}) {
+    CGTune cand = best;
+    cand.mv_tt = tt;
+    const float ms = time_it([&] {
+      launch_cg_matvec(p.v(), g.v(), q.v(), d, k, st, c->dpart, c->stream, cand);
+    });
+    if (ms < bt) {
+      bt = ms;
+      best.mv_tt = tt;
+    }
+  }
+  bt = 1e30f;
+  const int pick_tt = best.mv_tt;
+  for (int ps : {4, 8, 16}) {
+    CGTune cand = best;
+    cand.per_sm = ps;
+    const float ms = time_it([&] {
+      launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, st, c->dpart, c->fpart,
+                       1 << 30, c->stream, cand);
+      launch_cg_direction(p.v(), r.v(), g.v(), d, k, st, c->stream, cand);
+    });
+    if (ms < bt) {
+      bt = ms;
+      best.per_sm = ps;
+    }
+  }
+  best.mv_tt = pick_tt;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  owner->tunes[key] = best;
+  return best;
+}
+
 void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
                       const float *i0w, const float *i1, const OFArgs &a, int *itersOut,
                       float *resOut) {
@@ -207,6 +280,7 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
   diag += a.wEnergy;
   k.diag = diag;
 
+  const CGTune tu = cg_tune(c, d, k);
   KLP(c, KC_ASSEMBLE, d.x, nint(d) * 8 + d.cells() * 64,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
@@ -218,14 +292,13 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
   for (;;) {
     const int n = (a.cgMaxIter - it) < chunk ? (a.cgMaxIter - it) : chunk;
     for (int s = 0; s < n; ++s) {
-      const int kk = it + s;
       KLP(c, KC_MATVEC, d.x, nint(d) * 48,
-          launch_cg_matvec(p.v(), g.v(), q.v(), d, k, c->st, c->dpart, c->stream));
+          launch_cg_matvec(p.v(), g.v(), q.v(), d, k, c->st, c->dpart, c->stream, tu));
       KLP(c, KC_UPDATE, d.x, nint(d) * 112,
           launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, c->st, c->dpart,
-                           c->fpart, kk, a.cgMaxIter, c->stream));
+                           c->fpart, a.cgMaxIter, c->stream, tu));
       KLP(c, KC_DIRECTION, d.x, nint(d) * 64,
-          launch_cg_direction(p.v(), r.v(), g.v(), d, k, c->st, c->stream));
+          launch_cg_direction(p.v(), r.v(), g.v(), d, k, c->st, c->stream, tu));
     }
     it += n;
     CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
@@ -558,6 +631,13 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
     if (kv.second.defo) grid_unpin(const_cast<flof_grid *>(kv.second.defo));
   }
   c->lats.clear();
+  // grids still alive: free their storage now and orphan the handles
+  for (flof_grid *g : c->grids) {
+    if (g->owned && g->d) cudaFree(g->d);
+    g->d = nullptr;
+    g->ctx = nullptr;
+  }
+  c->grids.clear();
   c->pool.release_all();
   cudaFree(c->st);
   cudaFreeHost(c->st_h);
@@ -573,7 +653,10 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (auto &kv : c->wsum_cache) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  for (flof_ctx *w : c->workers) flof_ctx_destroy(w);
   delete c;
+  // teardown reports nothing; leave no error behind for the next call
+  cudaGetLastError();
   return FLOF_OK;
 }
 
@@ -642,6 +725,10 @@ FLOF_API int flof_ctx_set_option(flof_ctx *c, int option, int value) {
     if (option == FLOF_OPT_CFL_SYNC) {
       need(value == 0 || value == 1, "FLOF_OPT_CFL_SYNC takes 0 or 1");
       c->cfl_force_sync = value;
+    } else if (option == FLOF_OPT_AUTOTUNE) {
+      need(value == 0 || value == 1, "FLOF_OPT_AUTOTUNE takes 0 or 1");
+      c->autotune = value;
+      for (flof_ctx *w : c->workers) w->autotune = value;
     } else {
       fail(FLOF_E_ARG, "unknown context option");
     }
@@ -653,6 +740,10 @@ FLOF_API int flof_ctx_trim(flof_ctx *c) {
     need(c != nullptr, "ctx is NULL");
     CK(cudaStreamSynchronize(c->stream));
     c->pool.trim();
+    for (flof_ctx *w : c->workers) {
+      CK(cudaStreamSynchronize(w->stream));
+      w->pool.trim();
+    }
   });
 }
 
@@ -678,6 +769,7 @@ FLOF_API int flof_grid_create(flof_ctx *c, const int dims[4], int elem, flof_gri
       fail(FLOF_E_OOM, "device allocation of a grid failed");
     }
     g->owned = true;
+    c->grids.insert(g);
     cudaError_t e2 = cudaMemsetAsync(g->d, 0, bytes, c->stream);
     if (e2 != cudaSuccess) {
       cudaFree(g->d);
@@ -704,6 +796,7 @@ FLOF_API int flof_grid_wrap(flof_ctx *c, const int dims[4], int elem, void *ptr,
     g->elem = elem;
     g->d = ptr;
     g->owned = false;
+    c->grids.insert(g);
     *out = g;
   });
 }
@@ -714,12 +807,7 @@ FLOF_API int flof_grid_destroy(flof_grid *g) {
     g->destroy_pending = true;
     return FLOF_OK;
   }
-  if (g->owned && g->d) {
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
-    cudaFree(g->d);
-  }
-  delete g;
+  grid_free(g);
   return FLOF_OK;
 }
 
@@ -1272,6 +1360,9 @@ LatsData &lats_of(flof_ctx *c, int id) {
   auto it = c->lats.find(id);
   if (it == c->lats.end() || !it->second.defo)
     fail(FLOF_E_STATE, "Load-advect data id " + std::to_string(id) + " not initialized!");
+  need(it->second.defo->ctx != nullptr,
+       "the deformation grid of load-advect id " + std::to_string(id) +
+           " belongs to a destroyed context");
   return it->second;
 }
 

@@ -9,10 +9,13 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <array>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/flof_gb300.h"
@@ -143,6 +146,17 @@ struct flof_ctx {
   int cfl_force_sync = 0;
   int profiling = 0;
   std::map<std::pair<uint32_t, int>, float *> wsum_cache;  // (sigma bits, radius)
+  // autotuned PCG launch shapes per grid size (FLOF_OPT_AUTOTUNE); worker
+  // contexts share their parent's table (tune_owner)
+  int autotune = 0;
+  std::map<std::array<int, 4>, flof::CGTune> tunes;
+  std::mutex tune_mu;
+  flof_ctx *tune_owner = nullptr;
+  // worker contexts of the batched solve (created on demand)
+  std::vector<flof_ctx *> workers;
+  // live grids of this context: destroying the context frees their storage
+  // and leaves the handles orphaned (ctx == nullptr) until they are destroyed
+  std::unordered_set<flof_grid *> grids;
   std::vector<fh::ProfRec> recs;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
@@ -168,11 +182,16 @@ struct flof_grid {
 
 namespace fh {
 
+// Frees a grid's storage (owned grids) and its handle.  A grid whose context
+// is gone has no storage left (the context freed it) and only the handle goes.
 inline void grid_free(flof_grid *g) {
-  if (g->owned && g->d) {
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
-    cudaFree(g->d);
+  if (g->ctx) {
+    if (g->owned && g->d) {
+      cudaSetDevice(g->ctx->device);
+      cudaStreamSynchronize(g->ctx->stream);
+      cudaFree(g->d);
+    }
+    g->ctx->grids.erase(g);
   }
   delete g;
 }
@@ -326,6 +345,9 @@ inline int guarded_host(F &&f) {
 
 template <class F>
 inline int guarded(F &&f) {
+  // an error left by an earlier call that had no way to report it (a
+  // teardown path) must not be charged to this one
+  cudaGetLastError();
   try {
     f();
     cudaError_t e = cudaGetLastError();
@@ -348,6 +370,7 @@ inline void need(bool cond, const std::string &msg) {
 }
 inline void need_grid(const flof_grid *g, const char *name) {
   need(g != nullptr, std::string(name) + " is NULL");
+  need(g->ctx != nullptr, std::string(name) + " belongs to a destroyed context");
   need(g->d != nullptr || g->cells() == 0, std::string(name) + " has no storage");
 }
 inline void same_size(const flof_grid *a, const flof_grid *b, const char *what) {

@@ -113,6 +113,13 @@ struct OFConsts {
 };
 
 int cg_blocks(Dims4 d);
+// Launch shapes of the PCG kernels, chosen per grid size by the autotuner
+// (defaults otherwise): t planes per matvec work item (4, 8 or 16) and
+// resident blocks per SM of the update / direction kernels.
+struct CGTune {
+  int mv_tt = 8;
+  int per_sm = 8;
+};
 // Assembly + PCG initialisation over all cells.  vel may be null (zero).
 // Writes g, r = rhs, p = z on the interior, zeros on the border ring, and
 // x = 0 everywhere.
@@ -122,13 +129,16 @@ void launch_of_assemble_init(const float *i0w, const float *i1,
                              float accuracy, CGState *st, double *dpart,
                              float *fpart, cudaStream_t s);
 void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
-                      OFConsts c, CGState *st, double *dpart, cudaStream_t s);
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
+                      const CGTune &tu = CGTune());
+// The update takes the iteration number from st->iters.
 void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
                       const float4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int iter, int maxIter,
-                      cudaStream_t s);
+                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+                      const CGTune &tu = CGTune());
 void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
-                         OFConsts c, CGState *st, cudaStream_t s);
+                         OFConsts c, CGState *st, cudaStream_t s,
+                         const CGTune &tu = CGTune());
 // vel = x / mDx over all cells (x border entries are zero)
 void launch_of_copy_back(const float4 *x, float4 *vel, long long cells,
                          float mDx, const CGState *st, cudaStream_t s);

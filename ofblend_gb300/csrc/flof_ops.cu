@@ -11,16 +11,15 @@
 
 namespace flof {
 
-static int g_sm_count = 0;
-
+// SM count of the current device, read once (thread-safe static init).
 int sm_count() {
-  if (g_sm_count == 0) {
-    int dev = 0;
+  static const int n = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sm_count <= 0) g_sm_count = 1;
-  }
-  return g_sm_count;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
 }
 
 int grid_for(long long n, int nt, int per_sm) {

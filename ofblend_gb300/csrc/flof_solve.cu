@@ -177,7 +177,6 @@ void launch_of_assemble_init(const float *i0w, const float *i1,
 // blocks per SM); p.Ap is accumulated per thread in float-float and summed
 // in double by the last block to finish, in a fixed order.
 constexpr int MV_NT = 128;
-constexpr int MV_TT = 8;
 
 struct MVShape {
   FastDiv fx;        // interior x extent
@@ -212,8 +211,8 @@ __device__ __forceinline__ void mv_load(MVLoads &a, const float4 *__restrict__ p
 }
 
 // OFFD: the neighbour terms are present (applyMat skips them for a zero
-// off-diagonal, optflow4d.cpp:215).
-template <bool OFFD>
+// off-diagonal, optflow4d.cpp:215).  MV_TT: t planes per work item.
+template <bool OFFD, int MV_TT>
 __global__ void __launch_bounds__(MV_NT)
 k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
             float4 *__restrict__ q, Dims4 d, MVShape sh, OFConsts c, CGState *st,
@@ -289,12 +288,15 @@ k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
   }
 }
 
-void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
-                      OFConsts c, CGState *st, double *dpart, cudaStream_t s) {
+namespace {
+
+template <bool OFFD, int TT>
+void matvec_variant(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFConsts c,
+                    CGState *st, double *dpart, cudaStream_t s) {
   MVShape sh;
   const int ex = d.x > 2 ? d.x - 2 : 1, ey = d.y > 2 ? d.y - 2 : 1;
   const int ez = d.z > 2 ? d.z - 2 : 1;
-  const int tchunks = d.t > 2 ? (d.t - 2 + MV_TT - 1) / MV_TT : 0;
+  const int tchunks = d.t > 2 ? (d.t - 2 + TT - 1) / TT : 0;
   const bool empty = d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3;
   sh.fx = FastDiv((uint32_t)ex);
   sh.nxy = empty ? 0 : ex * ey;
@@ -302,19 +304,37 @@ void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
   sh.fruns = FastDiv((uint32_t)sh.runs);
   sh.fz = FastDiv((uint32_t)ez);
   sh.items = empty ? 0 : sh.runs * ez * tchunks;
-  const bool offd = c.offd != 0.f;
-  static int per_sm[2] = {0, 0};
-  if (!per_sm[offd]) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm[offd], offd ? k_cg_matvec<true> : k_cg_matvec<false>, MV_NT, 0);
-    if (per_sm[offd] < 1) per_sm[offd] = 1;
-  }
-  int blocks = sm_count() * per_sm[offd];
+  // resident blocks per SM of this instantiation (computed once, thread-safe)
+  static const int per_sm = [] {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_matvec<OFFD, TT>, MV_NT, 0);
+    return n < 1 ? 1 : n;
+  }();
+  int blocks = sm_count() * per_sm;
   if (blocks > sh.items) blocks = sh.items > 0 ? sh.items : 1;
-  if (offd)
-    k_cg_matvec<true><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+  k_cg_matvec<OFFD, TT><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+}
+
+template <bool OFFD>
+void matvec_tt(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFConsts c, CGState *st,
+               double *dpart, cudaStream_t s, int tt) {
+  if (tt <= 4)
+    matvec_variant<OFFD, 4>(p, g, q, d, c, st, dpart, s);
+  else if (tt >= 16)
+    matvec_variant<OFFD, 16>(p, g, q, d, c, st, dpart, s);
   else
-    k_cg_matvec<false><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+    matvec_variant<OFFD, 8>(p, g, q, d, c, st, dpart, s);
+}
+
+}  // namespace
+
+void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
+                      const CGTune &tu) {
+  if (c.offd != 0.f)
+    matvec_tt<true>(p, g, q, d, c, st, dpart, s, tu.mv_tt);
+  else
+    matvec_tt<false>(p, g, q, d, c, st, dpart, s, tu.mv_tt);
 }
 
 // x += alpha p; r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).
@@ -322,8 +342,7 @@ __global__ void __launch_bounds__(NT)
 k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
             const float4 *__restrict__ p, const float4 *__restrict__ q,
             const float4 *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
-            OFConsts c, CGState *st, double *dpart, float *fpart, int iter,
-            int maxIter) {
+            OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
   if (st->done) return;
   __shared__ double shd[NT / 32];
   __shared__ float shf[NT / 32];
@@ -371,6 +390,7 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
     m = block_max<NT>(m, shf);
     if (threadIdx.x == 0) {
       const double residual = (double)m;
+      const int iter = st->iters;
       st->resMax = m;
       st->retResidual = (float)(residual / st->resIni);
       st->iters = iter + 1;
@@ -388,11 +408,11 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
 
 void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
                       const float4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int iter, int maxIter,
-                      cudaStream_t s) {
-  k_cg_update<<<cg_blocks(d), NT, 0, s>>>(x, r, p, q, g, d, interior_decoder(d),
-                                          interior_count(d), c, st, dpart, fpart,
-                                          iter, maxIter);
+                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+                      const CGTune &tu) {
+  const long long n = interior_count(d);
+  k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
+      x, r, p, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
 }
 
 // p = z + beta p
@@ -419,9 +439,10 @@ k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
 }
 
 void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
-                         OFConsts c, CGState *st, cudaStream_t s) {
-  k_cg_direction<<<cg_blocks(d), NT, 0, s>>>(p, r, g, d, interior_decoder(d),
-                                             interior_count(d), c, st);
+                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
+  const long long n = interior_count(d);
+  k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
+      p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
 }
 
 // vel = x / mDx (optflow4d.cpp:520-529); a NaN residual resets the result to

@@ -264,12 +264,12 @@ static void launch_slab(const float *src, float *dst, Dims4 d, const float *wsum
   const size_t smem = 2 * G::SLOTS * sizeof(T);
   WTab2 wt;
   for (int i = 0; i < 40; ++i) wt.w[i] = (w && i <= 4 * S * S) ? w[i] : 0.f;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static const bool attr_set = [] {
     cudaFuncSetAttribute(k_slab_stencil<S, NC, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)smem);
-    attr_set = true;
-  }
+                         (int)(2 * SlabGeom<S>::SLOTS * sizeof(typename VT<NC>::T)));
+    return true;
+  }();
+  (void)attr_set;
   k_slab_stencil<S, NC, MODE><<<grid, NTHREADS, smem, st>>>(src, dst, d, tiles_x, wsum, mark, wt,
                                                             zero_border);
 }

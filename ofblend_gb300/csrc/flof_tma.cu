@@ -292,19 +292,17 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // looked up once (thread-safe static init); null when the driver lacks it
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
                                          &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    else
-      cudaGetLastError();
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    cudaGetLastError();
+    return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+  }();
   return fn;
 }
 
@@ -335,15 +333,15 @@ bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
   const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + G::TY - 1) / G::TY;
   dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
   const size_t smem = G::SMEM;
-  static bool attr = false;
-  if (!attr) {
+  static const bool attr = [] {
     if (cudaFuncSetAttribute(k_slab_tma<S, MODE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess) {
+                             (int)G::SMEM) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
-    attr = true;
-  }
+    return true;
+  }();
+  if (!attr) return false;
   WTabT wt;
   for (int i = 0; i < 40; ++i) wt.w[i] = (w && i <= 4 * S * S) ? w[i] : 0.f;
   k_slab_tma<S, MODE, G><<<grid, G::NTHR, smem, st>>>(map, dst, d, tiles_x, wsum, fixed, wt,

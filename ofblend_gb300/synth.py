@@ -128,3 +128,22 @@ def random_pair_scenes(seed: int, ndrops_range=(1, 3), radius_range=(3.0, 8.0)):
     s1 = make_scene(int(rng.integers(1 << 30)), kind=k1, ndrops=n1, radius_range=radius_range,
                     axes_range=radius_range)
     return s0, s1
+
+
+BATCH_SIZES = (24, 32, 40, 48, 64)
+BATCH_T = (16, 32, 48)
+
+
+def batch_pairs(n: int = 64, base_seed: int = 1000):
+    """n deformation pairs of uneven sizes: spatial resolution from
+    BATCH_SIZES and t extent from BATCH_T, 1-3 drops of radius U(3, 8) per
+    data set; pair k draws from seed base_seed + k.  Returns a list of
+    (dims, scene0, scene1) with dims = (S, S, S, T)."""
+    out = []
+    for k in range(n):
+        rng = np.random.default_rng(base_seed + k)
+        S = int(BATCH_SIZES[int(rng.integers(0, len(BATCH_SIZES)))])
+        T = int(BATCH_T[int(rng.integers(0, len(BATCH_T)))])
+        s0, s1 = random_pair_scenes(base_seed + k)
+        out.append(((S, S, S, T), s0, s1))
+    return out
