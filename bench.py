@@ -50,9 +50,10 @@ def args_():
     ap.add_argument("--blur-type", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="flof", choices=["flof", "batch"],
+    ap.add_argument("--workload", default="flof", choices=["flof", "batch", "mixed"],
                     help="flof: the two-way 64^4 workload (default); batch: 64 independent solves of "
-                         "uneven sizes, concurrent against sequential")
+                         "uneven sizes, concurrent against sequential; mixed: the 96^4 solve in mixed "
+                         "precision against FP32")
     ap.add_argument("--batch-pairs", type=int, default=64)
     ap.add_argument("--batch-workers", type=int, default=0)
     return ap.parse_args()
@@ -476,11 +477,71 @@ def run_batch(a):
     ctx.close()
 
 
+def run_mixed(a):
+    """Mixed precision (BF16 gradient, FP64 residuals, iterative refinement)
+    against the FP32 solve at 96^4 with two drops per data set.  The errors
+    against the FP64 oracle are measured by tests/test_gpu_batch.py."""
+    import torch
+    import ofblend_gb300 as F
+    from ofblend_gb300 import synth
+    torch.cuda.set_device(0)
+    ctx = F.Context(0)
+    p = dict(flof_params(a.cg_accuracy, a.blur_type), doFinalProject=False)
+
+    def scenes():
+        return (synth.make_scene(11, ndrops=2, radius_range=(4.0, 6.0)),
+                synth.make_scene(12, ndrops=2, radius_range=(4.0, 6.0)))
+
+    s0, s1 = scenes()
+    R = 96
+    dims = (R, R, R, R)
+    g0 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(synth.flow_input(s0, dims))
+    g1 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(synth.flow_input(s1, dims))
+    v = F.Grid4Vec4(dims=dims, ctx=ctx)
+    res = {}
+    for prec in ("fp32", "mixed"):
+        for _ in range(max(a.warmup, 1)):
+            v.setConst(0.0)
+            F.opticalFlowMultiscale4d(v, g0, g1, precision=prec, **p)
+        times = []
+        for _ in range(max(a.steps, 1)):
+            v.setConst(0.0)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            F.opticalFlowMultiscale4d(v, g0, g1, precision=prec, **p)
+            ctx.synchronize()
+            times.append(time.perf_counter() - t0)
+        st = F.last_solve_stats()
+        res[prec] = {"s": min(times), "vel": v.to_numpy(), "stats": st}
+    d96 = float(np.linalg.norm(res["mixed"]["vel"] - res["fp32"]["vel"]) /
+                np.linalg.norm(res["fp32"]["vel"]))
+
+    m = res["mixed"]["stats"]
+    line = {
+        "metric": "4D flow solves/s at 96^4, mixed precision (BF16 gradient, FP64 refinement)",
+        "value": round(1.0 / res["mixed"]["s"], 4), "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(res["mixed"]["s"] * 1e3, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16/f32/f64",
+        "data": "synthetic (two drops per data set)",
+        "config": {"workload": "one deformation 96^4, flof parameters without the final projection, "
+                               f"cgAccuracy {a.cg_accuracy}", "grid": [96] * 4},
+        "fp32": {"value": round(1.0 / res["fp32"]["s"], 4), "ms": round(res["fp32"]["s"] * 1e3, 2),
+                 "cg_iterations": res["fp32"]["stats"]["cg_total_iterations"]},
+        "mixed_cg_iterations": m["cg_total_iterations"],
+        "mixed_true_residual_finest": m["true_residual"][-1] if m["true_residual"] else None,
+        "mixed_vs_fp32_rel_l2_96": d96,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = args_()
     if a.impl == "reference":
         run_reference(a)
     elif a.workload == "batch":
         run_batch(a)
+    elif a.workload == "mixed":
+        run_mixed(a)
     else:
         run_gpu(a)

@@ -78,8 +78,14 @@ typedef struct flof_of_params {
   int minGridSize;
   int doFinalProject;
   int cgMaxIter;
-  int reserved[7];
+  /* FLOF_PRECISION_FP32 (default): the reference's float solve.
+   * FLOF_PRECISION_MIXED: PCG on the BF16-stored image gradient, FP64
+   * residuals of the FP32 system and iterative refinement (no reference
+   * counterpart). */
+  int precision;
+  int reserved[6];
 } flof_of_params;
+enum { FLOF_PRECISION_FP32 = 0, FLOF_PRECISION_MIXED = 1 };
 
 #define FLOF_MAX_SOLVE_STATS 64
 /* Per-call record of the linear solves (the reference logs the same facts
@@ -96,6 +102,9 @@ typedef struct flof_solve_stats {
   int syncs;                            /* host synchronisations            */
   float err_final;                      /* returned error metric            */
   double seconds;                       /* wall time of the call            */
+  /* ||b - A x||_2 / ||b||_2 of the FP32 system in FP64 (mixed precision;
+   * -1 when not computed) */
+  float true_residual[FLOF_MAX_SOLVE_STATS];
 } flof_solve_stats;
 
 /* ---- library / context -------------------------------------------------- */

@@ -16,6 +16,8 @@ FLOF_REAL = 1
 FLOF_VEC4 = 8
 FLOF_OPT_CFL_SYNC = 2
 FLOF_OPT_AUTOTUNE = 3
+FLOF_PRECISION_FP32 = 0
+FLOF_PRECISION_MIXED = 1
 MAX_SOLVE_STATS = 64
 
 STATUS = {
@@ -40,7 +42,7 @@ class OFParams(ctypes.Structure):
         ("resetBndWidth", ctypes.c_float), ("multiStep", ctypes.c_int),
         ("projSizeThresh", ctypes.c_int), ("minGridSize", ctypes.c_int),
         ("doFinalProject", ctypes.c_int), ("cgMaxIter", ctypes.c_int),
-        ("reserved", ctypes.c_int * 7),
+        ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 6),
     ]
 
 
@@ -55,6 +57,7 @@ class SolveStats(ctypes.Structure):
         ("syncs", ctypes.c_int),
         ("err_final", ctypes.c_float),
         ("seconds", ctypes.c_double),
+        ("true_residual", ctypes.c_float * MAX_SOLVE_STATS),
     ]
 
     def as_dict(self) -> dict:
@@ -67,6 +70,7 @@ class SolveStats(ctypes.Structure):
             "syncs": self.syncs,
             "err_final": float(self.err_final),
             "seconds": float(self.seconds),
+            "true_residual": [float(self.true_residual[q]) for q in range(n)],
         }
 
 

@@ -366,7 +366,7 @@ def _ctx_of(g) -> Context:
 
 def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e-04, blurType=1, cfl=999,
                orderTime=1, orderSpace=1, resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999,
-               minGridSize=10, doFinalProject=False, cgMaxIter=1000):
+               minGridSize=10, doFinalProject=False, cgMaxIter=1000, precision="fp32"):
     p = OFParams()
     _lib.lib().flof_of_params_default(ctypes.byref(p))
     p.wSmooth, p.wEnergy, p.level = wSmooth, wEnergy, int(level)
@@ -375,18 +375,25 @@ def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e
     p.resetBndWidth, p.multiStep = resetBndWidth, int(multiStep)
     p.projSizeThresh, p.minGridSize = int(projSizeThresh), int(minGridSize)
     p.doFinalProject, p.cgMaxIter = int(bool(doFinalProject)), int(cgMaxIter)
+    prec = {"fp32": _lib.FLOF_PRECISION_FP32, "mixed": _lib.FLOF_PRECISION_MIXED}
+    if precision not in prec:
+        raise FlofError(1, "precision must be 'fp32' or 'mixed'")
+    p.precision = prec[precision]
     return p
 
 
 def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
                             cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
                             resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
-                            doFinalProject=False, cgMaxIter=1000):
+                            doFinalProject=False, cgMaxIter=1000, precision="fp32"):
     """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
-    error metric (the reference's template returns it to C++ callers)."""
+    error metric (the reference's template returns it to C++ callers).
+    precision="mixed" solves with the BF16-stored gradient and FP64
+    iterative refinement (no reference counterpart)."""
     global _last_stats
     p = _of_params(wSmooth, wEnergy, level, postVelBlur, cgAccuracy, blurType, cfl, orderTime, orderSpace,
-                   resetBndWidth, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter)
+                   resetBndWidth, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter,
+                   precision)
     err = ctypes.c_float()
     st = SolveStats()
     ctx = _ctx_of(vel)

@@ -270,6 +270,23 @@ __device__ __forceinline__ float interp3_real(const float *__restrict__ data, co
              f1;
 }
 
+// ---- BF16 storage of Vec4 data ----------------------------------------------------
+
+// Four bfloat16 values (x, y, z, w) in 8 bytes.  bf16 -> float is exact (the
+// bf16 bits are the top half of the float); float -> bf16 rounds to nearest
+// even (to_bf4).
+struct __align__(8) BF4 {
+  unsigned short x, y, z, w;
+};
+__device__ __forceinline__ float4 ld_g(const float4 *__restrict__ g, idx_t i) {
+  return __ldg(g + i);
+}
+__device__ __forceinline__ float4 ld_g(const BF4 *__restrict__ g, idx_t i) {
+  const uint2 u = __ldg((const uint2 *)(g + i));
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                     __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+
 // ---- compensated accumulation ------------------------------------------------
 
 // Float-float accumulator (Knuth's TwoSum): `hi` carries the running sum,

@@ -185,6 +185,7 @@ void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurTyp
 struct OFArgs {
   float wSmooth, wEnergy, postVelBlur, cgAccuracy, resetBndWidth;
   int blurType, cgMaxIter;
+  int precision = FLOF_PRECISION_FP32;
 };
 
 // opticalFlowDim<Grid4d<Real>,Grid4d<Vec4>,4> (optflow4d.cpp:361-553).
@@ -263,6 +264,111 @@ CGTune cg_tune(flof_ctx *c, Dims4 d, const OFConsts &k) {
   return best;
 }
 
+// PCG iterations (GridCGOptflow4d::solve, optflow4d.cpp:304-326) from the
+// state the initialisation left.  Iterations are launched in chunks without
+// waiting; every kernel returns at once when the state says done.  After each
+// chunk the host reads the state (into c->st_h) and sizes the next chunk from
+// the observed reduction rate.
+template <class GT>
+void pcg_loop(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *x, float4 *r,
+              float4 *p, float4 *q, const GT *g, int maxIter) {
+  const double gb = sizeof(GT) == 8 ? 8.0 : 16.0;  // bytes of g per cell
+  int it = 0;
+  int chunk = 4;
+  for (;;) {
+    const int n = (maxIter - it) < chunk ? (maxIter - it) : chunk;
+    for (int s = 0; s < n; ++s) {
+      KLP(c, KC_MATVEC, d.x, nint(d) * (32 + gb),
+          launch_cg_matvec(p, g, q, d, k, c->st, c->dpart, c->stream, tu));
+      KLP(c, KC_UPDATE, d.x, nint(d) * (96 + gb),
+          launch_cg_update(x, r, p, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream,
+                           tu));
+      KLP(c, KC_DIRECTION, d.x, nint(d) * (48 + gb),
+          launch_cg_direction(p, r, g, d, k, c->st, c->stream, tu));
+    }
+    it += n;
+    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (c->st_h->done != CG_RUNNING) break;
+    if (it >= maxIter) break;
+    const double ratio = (double)c->st_h->resMax / c->st_h->resIni;
+    const double target = c->st_h->acc / c->st_h->resIni;
+    if (ratio > 0 && ratio < 1 && target > 0) {
+      const double rate = log(ratio) / it;
+      const double est = rate < 0 ? (log(target) - log(ratio)) / rate : 64;
+      const int e = (int)(est * 1.1) + 2;
+      chunk = e < 2 ? 2 : (e > 64 ? 64 : e);
+    } else {
+      chunk = chunk * 2 > 64 ? 64 : chunk * 2;
+    }
+  }
+}
+
+// Mixed-precision solve with iterative refinement.  The PCG runs on the
+// matrix of the BF16-stored gradient, first to sqrt(cgAccuracy) (restarting
+// from the assembly's r = b with that matrix's preconditioner).  Then, up to
+// MAX_REFINE times: r = b - A x of the FP32 matrix with FP64 row sums; stop
+// when the reference's criterion holds for this true residual (signed max
+// <= cgAccuracy x the signed max of b); else solve the BF16 system for the
+// correction just far enough to meet it (at least 10x, at most 1000x) and
+// add it in FP64.  Each refinement restarts the Krylov space, so the
+// accuracy is split between the solves instead of demanded of each.  The true
+// relative residual ||b - A x|| / ||b|| (FP64) goes to the solve record.
+void mixed_solve(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, const OFArgs &a,
+                 const float4 *g, float4 *x, float4 *r, float4 *p, float4 *q, int *itersOut,
+                 float *resOut) {
+  constexpr int MAX_REFINE = 4;
+  const size_t vb = vec_bytes(d);
+  DBuf g16(c, (size_t)d.cells() * sizeof(BF4)), b(c, vb), e(c, vb);
+  CK(cudaMemcpyAsync(b.p, r, vb, cudaMemcpyDeviceToDevice, c->stream));
+  KLP(c, KC_ELEMWISE, d.x, d.cells() * 24,
+      launch_to_bf4(g, (BF4 *)g16.p, d.cells(), c->stream));
+  const BF4 *gh = (const BF4 *)g16.p;
+  const float first_acc = a.cgAccuracy < 1e-2f ? sqrtf(a.cgAccuracy) : a.cgAccuracy;
+  KLP(c, KC_ASSEMBLE, d.x, nint(d) * 40,
+      launch_cg_init_r(r, gh, p, d, k, first_acc, c->st, c->dpart, c->fpart, c->stream));
+  pcg_loop(c, d, k, tu, x, r, p, q, gh, a.cgMaxIter);
+  int status = c->st_h->done;
+  if (status == CG_RUNNING) status = CG_MAXITER;
+  int iters = c->st_h->iters;
+  const float res = c->st_h->retResidual;
+  const double bmax = c->st_h->resIni;  // signed max of b
+  double true_rel = -1.0;
+  auto true_residual = [&]() {
+    CK(cudaMemsetAsync(c->dres + 8, 0, 2 * sizeof(double), c->stream));
+    KLP(c, KC_UPDATE, d.x, nint(d) * 64,
+        launch_residual64(x, b.v(), g, r, d, k, c->dpart, c->counter + 7, c->dres + 8,
+                          c->fres + 8, c->stream));
+    CK(cudaMemcpyAsync(c->dres_h + 8, c->dres + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaMemcpyAsync(c->fres_h + 10, c->fres + 8, sizeof(float), cudaMemcpyDeviceToHost,
+                       c->stream));
+    sync(c);
+    true_rel = c->dres_h[9] > 0 ? sqrt(c->dres_h[8] / c->dres_h[9]) : 0.0;
+    return (double)c->fres_h[10];
+  };
+  if (status == CG_CONVERGED || status == CG_MAXITER) {
+    for (int ref = 0; ref < MAX_REFINE; ++ref) {
+      const double rmax = true_residual();
+      const double goal = (double)a.cgAccuracy * bmax;
+      if (!(rmax > goal)) break;
+      double inner = 0.5 * goal / rmax;  // the reduction still needed, with margin
+      inner = inner > 0.1 ? 0.1 : (inner < 1e-3 ? 1e-3 : inner);
+      CK(cudaMemsetAsync(e.p, 0, vb, c->stream));
+      KLP(c, KC_ASSEMBLE, d.x, nint(d) * 40,
+          launch_cg_init_r(r, gh, p, d, k, (float)inner, c->st, c->dpart, c->fpart, c->stream));
+      pcg_loop(c, d, k, tu, e.v(), r, p, q, gh, a.cgMaxIter);
+      iters += c->st_h->iters;
+      KLP(c, KC_ELEMWISE, d.x, d.cells() * 48,
+          launch_add_correction(x, e.v(), d.cells(), c->stream));
+    }
+    true_residual();
+  }
+  record_solve(c, d.x, iters, res, status, (float)true_rel);
+  if (itersOut) *itersOut = iters;
+  if (resOut) *resOut = res;
+}
+
 void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
                       const float *i0w, const float *i1, const OFArgs &a, int *itersOut,
                       float *resOut) {
@@ -284,45 +390,18 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
   KLP(c, KC_ASSEMBLE, d.x, nint(d) * 8 + d.cells() * 64,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
-  // Iterations are launched in chunks without waiting; every kernel returns
-  // at once when the state says done.  After each chunk the host reads the
-  // state and sizes the next chunk from the observed reduction rate.
-  int it = 0;
-  int chunk = 4;
-  for (;;) {
-    const int n = (a.cgMaxIter - it) < chunk ? (a.cgMaxIter - it) : chunk;
-    for (int s = 0; s < n; ++s) {
-      KLP(c, KC_MATVEC, d.x, nint(d) * 48,
-          launch_cg_matvec(p.v(), g.v(), q.v(), d, k, c->st, c->dpart, c->stream, tu));
-      KLP(c, KC_UPDATE, d.x, nint(d) * 112,
-          launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, c->st, c->dpart,
-                           c->fpart, a.cgMaxIter, c->stream, tu));
-      KLP(c, KC_DIRECTION, d.x, nint(d) * 64,
-          launch_cg_direction(p.v(), r.v(), g.v(), d, k, c->st, c->stream, tu));
-    }
-    it += n;
-    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
-    sync(c);
-    if (c->st_h->done != CG_RUNNING) break;
-    if (it >= a.cgMaxIter) break;
-    const double ratio = (double)c->st_h->resMax / c->st_h->resIni;
-    const double target = c->st_h->acc / c->st_h->resIni;
-    if (ratio > 0 && ratio < 1 && target > 0) {
-      const double rate = log(ratio) / it;
-      const double est = rate < 0 ? (log(target) - log(ratio)) / rate : 64;
-      const int e = (int)(est * 1.1) + 2;
-      chunk = e < 2 ? 2 : (e > 64 ? 64 : e);
-    } else {
-      chunk = chunk * 2 > 64 ? 64 : chunk * 2;
-    }
+  if (a.precision != FLOF_PRECISION_MIXED) {
+    pcg_loop(c, d, k, tu, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter);
+    int status = c->st_h->done;
+    if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
+    const int iters = c->st_h->iters;
+    const float res = c->st_h->retResidual;
+    record_solve(c, d.x, iters, res, status);
+    if (itersOut) *itersOut = iters;
+    if (resOut) *resOut = res;
+  } else {
+    mixed_solve(c, d, k, tu, a, g.v(), x.v(), r.v(), p.v(), q.v(), itersOut, resOut);
   }
-  int status = c->st_h->done;
-  if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
-  const int iters = c->st_h->iters;
-  const float res = c->st_h->retResidual;
-  record_solve(c, d.x, iters, res, status);
-  if (itersOut) *itersOut = iters;
-  if (resOut) *resOut = res;
 
   KLP(c, KC_COPYBACK, d.x, d.cells() * 32,
       launch_of_copy_back(x.v(), velOut, d.cells(), k.mDx, c->st, c->stream));
@@ -400,6 +479,7 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
 struct MSArgs {
   float wSmooth, wEnergy, postVelBlur, cgAccuracy, cfl, resetBndWidth;
   int blurType, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter;
+  int precision = FLOF_PRECISION_FP32;
 };
 
 // opticalFlowMultiscaleTemplate (optflow4d.cpp:936-1173).
@@ -417,6 +497,7 @@ float multiscale(flof_ctx *c, Dims4 d, float4 *vel, const float *i0, const float
   oa.resetBndWidth = p.resetBndWidth;
   oa.blurType = p.blurType;
   oa.cgMaxIter = p.cgMaxIter;
+  oa.precision = p.precision;
 
   DBuf i0warped(c, real_bytes(d));
   CK(cudaMemcpyAsync(i0warped.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
@@ -986,6 +1067,8 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     need(pp.blurType == 1 || pp.blurType == 2, "blurType must be 1 or 2");
     need(pp.cgMaxIter >= 0, "cgMaxIter must be >= 0");
     need(pp.cfl > 0.f, "cfl must be positive");
+    need(pp.precision == FLOF_PRECISION_FP32 || pp.precision == FLOF_PRECISION_MIXED,
+         "precision must be FLOF_PRECISION_FP32 or FLOF_PRECISION_MIXED");
     set_ctx_device(c);
     const auto t0 = std::chrono::steady_clock::now();
     flof_solve_stats local;
@@ -1005,6 +1088,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     m.minGridSize = pp.minGridSize;
     m.doFinalProject = pp.doFinalProject;
     m.cgMaxIter = pp.cgMaxIter;
+    m.precision = pp.precision;
     float e;
     try {
       // speculative pass: CFL substep counts checked on the device

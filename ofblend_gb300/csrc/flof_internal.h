@@ -307,7 +307,8 @@ inline void check_device_errors(flof_ctx *c) {
   }
 }
 
-inline void record_solve(flof_ctx *c, int sx, int iters, float res, int status) {
+inline void record_solve(flof_ctx *c, int sx, int iters, float res, int status,
+                         float true_res = -1.f) {
   flof_solve_stats *s = c->stats;
   if (!s) return;
   if (s->nsolves < FLOF_MAX_SOLVE_STATS) {
@@ -315,6 +316,7 @@ inline void record_solve(flof_ctx *c, int sx, int iters, float res, int status) 
     s->iterations[s->nsolves] = iters;
     s->residual[s->nsolves] = res;
     s->status[s->nsolves] = status;
+    s->true_residual[s->nsolves] = true_res;
   }
   s->nsolves++;
   s->cg_total_iterations += iters > 0 ? iters : 0;

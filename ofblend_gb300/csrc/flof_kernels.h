@@ -139,6 +139,35 @@ void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
 void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s,
                          const CGTune &tu = CGTune());
+// The same three kernels with the image gradient stored in BF16 (mixed
+// precision: the matrix g g^T + diag I is built from the rounded gradient).
+void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
+                      const CGTune &tu = CGTune());
+void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
+                      const BF4 *g, Dims4 d, OFConsts c, CGState *st,
+                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+                      const CGTune &tu = CGTune());
+void launch_cg_direction(float4 *p, const float4 *r, const BF4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s,
+                         const CGTune &tu = CGTune());
+// ---- mixed precision (flof_mixed.cu) ------------------------------------------
+// g16 = bf16(g) over n cells
+void launch_to_bf4(const float4 *g, BF4 *g16, long long n, cudaStream_t s);
+// r = b - A x over the interior with A built from the FP32 gradient g and the
+// row sums accumulated in FP64; res[0] = ||r||^2, res[1] = ||b||^2 (FP64),
+// fres[0] = signed max of r (0 included: border rows).  res/fres must be
+// zeroed (reset by the kernel's last block for the next call).
+void launch_residual64(const float4 *x, const float4 *b, const float4 *g, float4 *r, Dims4 d,
+                       OFConsts c, double *dpart, unsigned int *counter, double *res,
+                       float *fres, cudaStream_t s);
+// PCG start from a given residual r (x0 = 0, the caller zeroes x): p = z =
+// M^-1 r on the interior, sigma = z.r, resIni = signed max of r; the state
+// logic of the assembly's initialisation.
+void launch_cg_init_r(const float4 *r, const BF4 *g, float4 *p, Dims4 d, OFConsts c,
+                      float accuracy, CGState *st, double *dpart, float *fpart, cudaStream_t s);
+// x = float((double)x + (double)e) over n cells
+void launch_add_correction(float4 *x, const float4 *e, long long n, cudaStream_t s);
 // vel = x / mDx over all cells (x border entries are zero)
 void launch_of_copy_back(const float4 *x, float4 *vel, long long cells,
                          float mDx, const CGState *st, cudaStream_t s);

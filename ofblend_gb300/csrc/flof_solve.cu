@@ -197,11 +197,12 @@ __device__ __forceinline__ void mv_acc(float4 &v, float o, const float4 a) {
 struct MVLoads {
   float4 pp, gg, zm, ym, xm, xp, yp, zp;
 };
+template <class GT>
 __device__ __forceinline__ void mv_load(MVLoads &a, const float4 *__restrict__ p,
-                                        const float4 *__restrict__ g, idx_t id, idx_t sY,
+                                        const GT *__restrict__ g, idx_t id, idx_t sY,
                                         idx_t sZ, idx_t sT) {
   a.pp = __ldg(p + id + sT);
-  a.gg = __ldg(g + id);
+  a.gg = ld_g(g, id);
   a.zm = __ldg(p + id - sZ);
   a.ym = __ldg(p + id - sY);
   a.xm = __ldg(p + id - 1);
@@ -212,9 +213,9 @@ __device__ __forceinline__ void mv_load(MVLoads &a, const float4 *__restrict__ p
 
 // OFFD: the neighbour terms are present (applyMat skips them for a zero
 // off-diagonal, optflow4d.cpp:215).  MV_TT: t planes per work item.
-template <bool OFFD, int MV_TT>
+template <bool OFFD, int MV_TT, class GT>
 __global__ void __launch_bounds__(MV_NT)
-k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
+k_cg_matvec(const float4 *__restrict__ p, const GT *__restrict__ g,
             float4 *__restrict__ q, Dims4 d, MVShape sh, OFConsts c, CGState *st,
             double *dpart) {
   if (st->done) return;
@@ -290,8 +291,8 @@ k_cg_matvec(const float4 *__restrict__ p, const float4 *__restrict__ g,
 
 namespace {
 
-template <bool OFFD, int TT>
-void matvec_variant(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFConsts c,
+template <bool OFFD, int TT, class GT>
+void matvec_variant(const float4 *p, const GT *g, float4 *q, Dims4 d, OFConsts c,
                     CGState *st, double *dpart, cudaStream_t s) {
   MVShape sh;
   const int ex = d.x > 2 ? d.x - 2 : 1, ey = d.y > 2 ? d.y - 2 : 1;
@@ -307,16 +308,16 @@ void matvec_variant(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFCons
   // resident blocks per SM of this instantiation (computed once, thread-safe)
   static const int per_sm = [] {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_matvec<OFFD, TT>, MV_NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg_matvec<OFFD, TT, GT>, MV_NT, 0);
     return n < 1 ? 1 : n;
   }();
   int blocks = sm_count() * per_sm;
   if (blocks > sh.items) blocks = sh.items > 0 ? sh.items : 1;
-  k_cg_matvec<OFFD, TT><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+  k_cg_matvec<OFFD, TT, GT><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
 }
 
-template <bool OFFD>
-void matvec_tt(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFConsts c, CGState *st,
+template <bool OFFD, class GT>
+void matvec_tt(const float4 *p, const GT *g, float4 *q, Dims4 d, OFConsts c, CGState *st,
                double *dpart, cudaStream_t s, int tt) {
   if (tt <= 4)
     matvec_variant<OFFD, 4>(p, g, q, d, c, st, dpart, s);
@@ -326,22 +327,34 @@ void matvec_tt(const float4 *p, const float4 *g, float4 *q, Dims4 d, OFConsts c,
     matvec_variant<OFFD, 8>(p, g, q, d, c, st, dpart, s);
 }
 
-}  // namespace
-
-void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
-                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
-                      const CGTune &tu) {
+template <class GT>
+void matvec_any(const float4 *p, const GT *g, float4 *q, Dims4 d, OFConsts c, CGState *st,
+                double *dpart, cudaStream_t s, const CGTune &tu) {
   if (c.offd != 0.f)
     matvec_tt<true>(p, g, q, d, c, st, dpart, s, tu.mv_tt);
   else
     matvec_tt<false>(p, g, q, d, c, st, dpart, s, tu.mv_tt);
 }
 
+}  // namespace
+
+void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
+                      const CGTune &tu) {
+  matvec_any(p, g, q, d, c, st, dpart, s, tu);
+}
+void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,
+                      OFConsts c, CGState *st, double *dpart, cudaStream_t s,
+                      const CGTune &tu) {
+  matvec_any(p, g, q, d, c, st, dpart, s, tu);
+}
+
 // x += alpha p; r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).
+template <class GT>
 __global__ void __launch_bounds__(NT)
 k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
             const float4 *__restrict__ p, const float4 *__restrict__ q,
-            const float4 *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
+            const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
             OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
   if (st->done) return;
   __shared__ double shd[NT / 32];
@@ -354,7 +367,7 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = __ldg(g + id);
+    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = ld_g(g, id);
     float4 xx = x[id], rr = r[id];
     xx.x = __fmaf_rn(a, pp.x, xx.x);
     xx.y = __fmaf_rn(a, pp.y, xx.y);
@@ -414,11 +427,20 @@ void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
   k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
       x, r, p, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
 }
+void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
+                      const BF4 *g, Dims4 d, OFConsts c, CGState *st,
+                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+                      const CGTune &tu) {
+  const long long n = interior_count(d);
+  k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
+      x, r, p, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
+}
 
 // p = z + beta p
+template <class GT>
 __global__ void __launch_bounds__(NT)
 k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
-               const float4 *__restrict__ g, Dims4 d, BoxDecoder bx,
+               const GT *__restrict__ g, Dims4 d, BoxDecoder bx,
                uint32_t nint, OFConsts c, CGState *st) {
   if (st->done) return;
   const float b = (float)st->beta;
@@ -427,7 +449,7 @@ k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    const float4 rr = __ldg(r + id), gg = __ldg(g + id);
+    const float4 rr = __ldg(r + id), gg = ld_g(g, id);
     float4 pp = p[id];
     const float4 pre = precond_of(gg, c.diag);
     pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
@@ -439,6 +461,12 @@ k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
 }
 
 void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
+  const long long n = interior_count(d);
+  k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
+      p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+}
+void launch_cg_direction(float4 *p, const float4 *r, const BF4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
   const long long n = interior_count(d);
   k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(

@@ -93,3 +93,36 @@ def test_grids_outliving_their_context(gpu):
     ctx2 = F.Context(0)  # no error left behind by the teardown
     F.Grid4Real(dims=(8, 8, 8, 8), ctx=ctx2).setConst(2.0)
     ctx2.close()
+
+
+# ---------------------------------------------------------------------------
+# mixed precision (BF16 gradient, FP64 residuals, iterative refinement)
+# ---------------------------------------------------------------------------
+def test_mixed_precision_against_fp64_oracle(gpu):
+    """The mixed solve's deformation against the FP64 oracle (the reference's
+    double build restated), next to the FP32 solve's; both must stay within
+    the deformation tolerance of each other's order, and the recorded true
+    residual of the FP32 system must be small."""
+    import oracle
+    o64 = oracle.get(double=True)
+    dims = (32, 32, 32, 32)
+    i0 = synth.flow_input(synth.scene_for(0), dims)
+    i1 = synth.flow_input(synth.scene_for(1), dims)
+    kw = dict(FLOF, cgAccuracy=1e-4, multiStep=1, doFinalProject=False)
+    zv = np.zeros(i0.shape + (4,), np.float64)
+    want = o64.opticalFlowMultiscale4d(zv, i0.astype(np.float64), i1.astype(np.float64),
+                                       **{k: v for k, v in kw.items() if k != "blurType"})[0]
+    out = {}
+    for prec in ("fp32", "mixed"):
+        v = F.Grid4Vec4(dims=dims)
+        F.opticalFlowMultiscale4d(v, F.Grid4Real(dims=dims).from_numpy(i0),
+                                  F.Grid4Real(dims=dims).from_numpy(i1), precision=prec, **kw)
+        out[prec] = (v.to_numpy().astype(np.float64), F.last_solve_stats())
+    rel = {p: np.linalg.norm(out[p][0] - want) / np.linalg.norm(want) for p in out}
+    print("rel L2 vs FP64 oracle:", rel, "true residual (mixed):", out["mixed"][1]["true_residual"],
+          "iterations:", {p: out[p][1]["cg_total_iterations"] for p in out})
+    assert rel["fp32"] < 1e-4, rel
+    assert rel["mixed"] < 1e-3, rel
+    tr = [t for t in out["mixed"][1]["true_residual"] if t >= 0]
+    assert tr and max(tr) < 1e-2, out["mixed"][1]
+    assert all(t < 0 for t in out["fp32"][1]["true_residual"])
