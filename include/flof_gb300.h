@@ -58,6 +58,7 @@ enum { FLOF_BLUR_GAUSS = 1, FLOF_BLUR_GAUSS_SEPARABLE = 2 };
 
 typedef struct flof_ctx flof_ctx;
 typedef struct flof_grid flof_grid;
+typedef struct flof_model flof_model;
 
 /* Keyword arguments of opticalFlowMultiscale4d
  * (optflow4d.cpp:2182-2189), same names and meaning, plus cgMaxIter, which
@@ -83,7 +84,11 @@ typedef struct flof_of_params {
    * residuals of the FP32 system and iterative refinement (no reference
    * counterpart). */
   int precision;
-  int reserved[6];
+  /* 1: start the coarsest level from the learned warm start attached with
+   * flof_ctx_set_model (dropped when it does not lower that level's error
+   * metric); 0 (default): the reference's zero start. */
+  int warmStart;
+  int reserved[5];
 } flof_of_params;
 enum { FLOF_PRECISION_FP32 = 0, FLOF_PRECISION_MIXED = 1 };
 
@@ -105,6 +110,9 @@ typedef struct flof_solve_stats {
   /* ||b - A x||_2 / ||b||_2 of the FP32 system in FP64 (mixed precision;
    * -1 when not computed) */
   float true_residual[FLOF_MAX_SOLVE_STATS];
+  /* learned warm start: 1 used, 0 dropped by the error check, -1 not tried */
+  int warm_start;
+  float warm_start_err[2];              /* coarse error: zero start, prediction */
 } flof_solve_stats;
 
 /* ---- library / context -------------------------------------------------- */
@@ -338,6 +346,37 @@ FLOF_API int flof_grid_save(const flof_grid *grid, const char *fname,
 /* readGrid4dUni(name, NULL, t, slice) (fileio.cpp:912-990): t slice of a 4D
  * file into a grid with the file's x, y, z extents and t extent 1. */
 FLOF_API int flof_uni_read_slice(flof_grid *slice, const char *fname, int t);
+
+/* ---- learned warm start ------------------------------------------------
+ * A 4D convolutional encoder-decoder (3 levels, 16/32/64 channels, BF16
+ * weights, FP32 accumulation) mapping the coarsest-level inputs (i0, i1) of
+ * the multiscale solve on a res^4 grid to that level's deformation.  It has
+ * no counterpart in the reference.  Training and inference run on the GPU;
+ * the plain PCG refines every level afterwards. */
+FLOF_API int flof_model_create(flof_ctx *ctx, int res, flof_model **out);
+FLOF_API int flof_model_destroy(flof_model *model);
+FLOF_API int flof_model_num_params(const flof_model *model, long long *n);
+/* He-normal weights from a seeded RNG, zero biases, fresh Adam state. */
+FLOF_API int flof_model_init(flof_model *model, unsigned long long seed);
+/* FP32 master parameters, layer by layer (weights [tap][cin][cout], bias). */
+FLOF_API int flof_model_get_params(const flof_model *model, float *host);
+FLOF_API int flof_model_set_params(flof_model *model, const float *host);
+/* vel (Vec4 res^4) = network(i0, i1) (Real res^4 grids). */
+FLOF_API int flof_model_predict(flof_model *model, const flof_grid *i0,
+                                const flof_grid *i1, flof_grid *vel);
+/* Mean squared error against target and its gradient (grad nullable, host,
+ * num_params floats) for one sample. */
+FLOF_API int flof_model_loss_grad(flof_model *model, const flof_grid *i0,
+                                  const flof_grid *i1, const flof_grid *target,
+                                  double *loss, float *grad);
+/* One Adam step on the mean loss of n samples. */
+FLOF_API int flof_model_train_step(flof_model *model, int n,
+                                   const flof_grid *const *i0s,
+                                   const flof_grid *const *i1s,
+                                   const flof_grid *const *targets, float lr,
+                                   double *loss);
+/* The model used when flof_of_params.warmStart is 1 (NULL detaches). */
+FLOF_API int flof_ctx_set_model(flof_ctx *ctx, flof_model *model);
 
 /* ---- input conditioning (scenes/flof.py postProcessPhiData :491-531) ---- */
 

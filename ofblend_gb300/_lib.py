@@ -42,7 +42,7 @@ class OFParams(ctypes.Structure):
         ("resetBndWidth", ctypes.c_float), ("multiStep", ctypes.c_int),
         ("projSizeThresh", ctypes.c_int), ("minGridSize", ctypes.c_int),
         ("doFinalProject", ctypes.c_int), ("cgMaxIter", ctypes.c_int),
-        ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 6),
+        ("precision", ctypes.c_int), ("warmStart", ctypes.c_int), ("reserved", ctypes.c_int * 5),
     ]
 
 
@@ -58,6 +58,8 @@ class SolveStats(ctypes.Structure):
         ("err_final", ctypes.c_float),
         ("seconds", ctypes.c_double),
         ("true_residual", ctypes.c_float * MAX_SOLVE_STATS),
+        ("warm_start", ctypes.c_int),
+        ("warm_start_err", ctypes.c_float * 2),
     ]
 
     def as_dict(self) -> dict:
@@ -71,6 +73,8 @@ class SolveStats(ctypes.Structure):
             "err_final": float(self.err_final),
             "seconds": float(self.seconds),
             "true_residual": [float(self.true_residual[q]) for q in range(n)],
+            "warm_start": self.warm_start,
+            "warm_start_err": (float(self.warm_start_err[0]), float(self.warm_start_err[1])),
         }
 
 
@@ -148,6 +152,16 @@ SIGNATURES = {
     "flof_loadAdvectTimeSlice_OptInitFile": (I, [P, I, ctypes.c_char_p, I, I, F]),
     "flof_loadAdvectTimeSlice": (I, [P, P, ctypes.c_char_p, P, P, F, F, F, P, P, P, P, F, I, F]),
     "flof_opticalFlowMultiscale4d_batch": (I, [P, I, P, P, P, P, FP, I]),
+    "flof_model_create": (I, [P, I, P]),
+    "flof_model_destroy": (I, [P]),
+    "flof_model_num_params": (I, [P, ctypes.POINTER(ctypes.c_longlong)]),
+    "flof_model_init": (I, [P, ctypes.c_ulonglong]),
+    "flof_model_get_params": (I, [P, P]),
+    "flof_model_set_params": (I, [P, P]),
+    "flof_model_predict": (I, [P, P, P, P]),
+    "flof_model_loss_grad": (I, [P, P, P, P, ctypes.POINTER(ctypes.c_double), P]),
+    "flof_model_train_step": (I, [P, I, P, P, P, F, ctypes.POINTER(ctypes.c_double)]),
+    "flof_ctx_set_model": (I, [P, P]),
 }
 
 _lib = None

@@ -35,7 +35,7 @@ __all__ = [
     "loadAdvectTimeSlice_OptRunTwoway", "loadAdvectTimeSlice_Finish", "last_solve_stats",
     "LevelsetGrid", "repeatFrame4d", "extrap4dLsSimple", "simpleBlurSpecial", "shiftForwGrid4d",
     "uniFileInfo", "getUniFileSize", "readGrid4dUniSlice", "loadPlaceGrid4d", "loadAdvectTimeSlice",
-    "opticalFlowMultiscale4d_batch",
+    "opticalFlowMultiscale4d_batch", "Model",
 ]
 
 
@@ -366,7 +366,7 @@ def _ctx_of(g) -> Context:
 
 def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e-04, blurType=1, cfl=999,
                orderTime=1, orderSpace=1, resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999,
-               minGridSize=10, doFinalProject=False, cgMaxIter=1000, precision="fp32"):
+               minGridSize=10, doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False):
     p = OFParams()
     _lib.lib().flof_of_params_default(ctypes.byref(p))
     p.wSmooth, p.wEnergy, p.level = wSmooth, wEnergy, int(level)
@@ -379,21 +379,23 @@ def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e
     if precision not in prec:
         raise FlofError(1, "precision must be 'fp32' or 'mixed'")
     p.precision = prec[precision]
+    p.warmStart = int(bool(warmStart))
     return p
 
 
 def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
                             cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
                             resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
-                            doFinalProject=False, cgMaxIter=1000, precision="fp32"):
+                            doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False):
     """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
     error metric (the reference's template returns it to C++ callers).
     precision="mixed" solves with the BF16-stored gradient and FP64
-    iterative refinement (no reference counterpart)."""
+    iterative refinement; warmStart=True starts the coarsest level from the
+    model attached with Model.attach (neither has a reference counterpart)."""
     global _last_stats
     p = _of_params(wSmooth, wEnergy, level, postVelBlur, cgAccuracy, blurType, cfl, orderTime, orderSpace,
                    resetBndWidth, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter,
-                   precision)
+                   precision, warmStart)
     err = ctypes.c_float()
     st = SolveStats()
     ctx = _ctx_of(vel)
@@ -637,3 +639,86 @@ def loadAdvectTimeSlice(dummyID, fname, dst, phi, time, blendAlpha, loadTimeScal
         ctx.h, defo, name, dst.h, phi.h, float(time), float(blendAlpha), float(loadTimeScale),
         f4(defoOffset), f4(defoScale), f4(defoFactor), f4(overrideSize if overrideSize is not None else -1.0),
         float(overrideTimeOff), int(bool(zeroVel)), float(defoAniFac)))
+
+
+# ---------------------------------------------------------------------------
+# learned warm start
+# ---------------------------------------------------------------------------
+class Model:
+    """The learned warm start: a 4D convolutional encoder-decoder mapping the
+    coarsest-level inputs (i0, i1 on a res^4 grid) of the multiscale solve to
+    that level's deformation.  Trained and evaluated on the GPU."""
+
+    def __init__(self, res: int = 16, ctx: Context | None = None, seed: int = 0):
+        self.ctx = ctx or context()
+        self.res = int(res)
+        h = ctypes.c_void_p()
+        check(self.ctx.lib.flof_model_create(self.ctx.h, self.res, ctypes.byref(h)))
+        self.h = h
+        self.init(seed)
+
+    def init(self, seed: int = 0):
+        check(self.ctx.lib.flof_model_init(self.h, ctypes.c_ulonglong(int(seed))))
+
+    @property
+    def num_params(self) -> int:
+        n = ctypes.c_longlong()
+        check(self.ctx.lib.flof_model_num_params(self.h, ctypes.byref(n)))
+        return int(n.value)
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        check(self.ctx.lib.flof_model_get_params(self.h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_params(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if a.size != self.num_params:
+            raise FlofError(1, f"expected {self.num_params} parameters, got {a.size}")
+        check(self.ctx.lib.flof_model_set_params(self.h, a.ctypes.data_as(ctypes.c_void_p)))
+
+    def save(self, path):
+        np.save(path, self.get_params())
+
+    def load(self, path):
+        self.set_params(np.load(path))
+        return self
+
+    def predict(self, i0, i1, vel):
+        check(self.ctx.lib.flof_model_predict(self.h, i0.h, i1.h, vel.h))
+        return vel
+
+    def loss_grad(self, i0, i1, target):
+        """(loss, gradient w.r.t. the parameters) of one sample."""
+        loss = ctypes.c_double()
+        g = np.empty(self.num_params, np.float32)
+        check(self.ctx.lib.flof_model_loss_grad(self.h, i0.h, i1.h, target.h, ctypes.byref(loss),
+                                                g.ctypes.data_as(ctypes.c_void_p)))
+        return float(loss.value), g
+
+    def train_step(self, samples, lr: float = 1e-3) -> float:
+        """One Adam step on the mean loss of [(i0, i1, target), ...]."""
+        n = len(samples)
+        arr = lambda k: (ctypes.c_void_p * n)(*[s[k].h.value for s in samples])
+        loss = ctypes.c_double()
+        check(self.ctx.lib.flof_model_train_step(self.h, n, arr(0), arr(1), arr(2), float(lr),
+                                                 ctypes.byref(loss)))
+        return float(loss.value)
+
+    def attach(self):
+        """Use this model when opticalFlowMultiscale4d is called with warmStart=True."""
+        check(self.ctx.lib.flof_ctx_set_model(self.ctx.h, self.h))
+
+    def detach(self):
+        check(self.ctx.lib.flof_ctx_set_model(self.ctx.h, None))
+
+    def free(self):
+        if getattr(self, "h", None) is not None:
+            self.ctx.lib.flof_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

@@ -480,6 +480,7 @@ struct MSArgs {
   float wSmooth, wEnergy, postVelBlur, cgAccuracy, cfl, resetBndWidth;
   int blurType, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter;
   int precision = FLOF_PRECISION_FP32;
+  int warmStart = 0;
 };
 
 // opticalFlowMultiscaleTemplate (optflow4d.cpp:936-1173).
@@ -514,6 +515,31 @@ float multiscale(flof_ctx *c, Dims4 d, float4 *vel, const float *i0, const float
     interpol_grid(c, (float *)vel, d, velSm.f(), sd, 4);
     KL(c, launch_mult_const((float *)vel, d.cells(), 4, make_float4(2.f, 2.f, 2.f, 2.f),
                             c->stream));
+  }
+
+  if (p.warmStart && !(d.x > p.minGridSize) && c->model) {
+    // learned warm start: the coarsest level starts from the network's
+    // prediction if that lowers the level's error metric, else as usual
+    const int R = model_res(c->model);
+    if (d.x == R && d.y == R && d.z == R && d.t == R) {
+      DBuf pred(c, vec_bytes(d)), tmp(c, real_bytes(d));
+      model_predict_raw(c->model, i0, i1, pred.v());
+      float err[2];
+      const float4 *cand[2] = {vel, pred.v()};
+      for (int q = 0; q < 2; ++q) {
+        CK(cudaMemcpyAsync(tmp.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+        advect_cfl(c, d, p.cfl, cand[q], tmp.f(), 1);
+        KLP(c, KC_BORDER, d.x, 0, launch_set_bound_neumann(tmp.f(), d, 1, 0, c->stream));
+        err[q] = ls_diff(c, tmp.f(), i1, nullptr, d, lsDiffFac, resetBnd);
+      }
+      const bool use = err[1] < err[0];
+      if (use) CK(cudaMemcpyAsync(vel, pred.p, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
+      if (c->stats) {
+        c->stats->warm_start = use ? 1 : 0;
+        c->stats->warm_start_err[0] = err[0];
+        c->stats->warm_start_err[1] = err[1];
+      }
+    }
   }
 
   advect_cfl(c, d, p.cfl, vel, i0warped.f(), 1);
@@ -712,6 +738,9 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
     if (kv.second.defo) grid_unpin(const_cast<flof_grid *>(kv.second.defo));
   }
   c->lats.clear();
+  for (flof_model *m : c->models) model_orphan(m);
+  c->models.clear();
+  c->model = nullptr;
   // grids still alive: free their storage now and orphan the handles
   for (flof_grid *g : c->grids) {
     if (g->owned && g->d) cudaFree(g->d);
@@ -1073,6 +1102,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     const auto t0 = std::chrono::steady_clock::now();
     flof_solve_stats local;
     memset(&local, 0, sizeof(local));
+    local.warm_start = -1;
     c->stats = &local;
     const int syncs0 = c->syncs;
     MSArgs m;
@@ -1089,6 +1119,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     m.doFinalProject = pp.doFinalProject;
     m.cgMaxIter = pp.cgMaxIter;
     m.precision = pp.precision;
+    m.warmStart = pp.warmStart;
     float e;
     try {
       // speculative pass: CFL substep counts checked on the device
@@ -1106,6 +1137,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
         // some advection needed more than one CFL substep: redo the call
         // with host-side substep counts
         memset(&local, 0, sizeof(local));
+        local.warm_start = -1;
         CK(cudaMemcpyAsync(vel->d, vel_in.p, vel->bytes(), cudaMemcpyDeviceToDevice, c->stream));
         c->cfl_sync = 1;
         e = multiscale(c, vel->D(), vel->v(), i0->f(), i1->f(), m, pp.level);

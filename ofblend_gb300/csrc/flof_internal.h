@@ -157,6 +157,9 @@ struct flof_ctx {
   // live grids of this context: destroying the context frees their storage
   // and leaves the handles orphaned (ctx == nullptr) until they are destroyed
   std::unordered_set<flof_grid *> grids;
+  // learned warm start used by the multiscale driver (flof_ctx_set_model)
+  flof_model *model = nullptr;
+  std::unordered_set<flof_model *> models;
   std::vector<fh::ProfRec> recs;
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
@@ -408,6 +411,14 @@ inline void grid_factor4d(const float s1[4], const float s2in[4], const float op
   }
 }
 
+}  // namespace fh
+
+// ---- learned warm start (flof_model.cu) -----------------------------------------
+namespace fh {
+void model_predict_raw(flof_model *m, const float *i0, const float *i1, float4 *vel);
+int model_res(const flof_model *m);
+// frees a model's device memory when its context goes (the handle stays)
+void model_orphan(flof_model *m);
 }  // namespace fh
 
 // ---- .uni files (flof_uni.cu) ----------------------------------------------------

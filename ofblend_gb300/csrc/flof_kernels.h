@@ -245,4 +245,27 @@ void launch_rescale_slices(float *phi, Dims4 d, const float *w, cudaStream_t s);
 // a += v over the bnd = 1 box of a 3D grid
 void launch_add_inner3(float *a, int X, int Y, int Z, float v, cudaStream_t s);
 
+// ---- learned warm start network (flof_net.cu) -----------------------------------
+// Channels-last tensors over cubic 4D grids; 3^4 (pad 1) or 1^4 convolutions.
+void net_conv_fwd(const float *in, const float *w, const float *b, float *out, int rin, int rout,
+                  int cin, int cout, int ks, int stride, int relu, cudaStream_t s);
+void net_conv_bwd_data(const float *dout, const float *w, float *din, int rin, int rout,
+                       int cin, int cout, int ks, int stride, cudaStream_t s);
+void net_conv_bwd_weight(const float *in, const float *dout, float *dw, int rin, int rout,
+                         int cin, int cout, int ks, int stride, cudaStream_t s);
+void net_relu_bwd(float *dy, const float *y, long long n, cudaStream_t s);
+void net_upcat(const float *lo, const float *skip, float *out, int R, int c1, int c2,
+               cudaStream_t s);
+void net_upcat_bwd(const float *dout, float *dlo, float *dskip, int R, int c1, int c2,
+                   cudaStream_t s);
+void net_bias_grad(const float *d, float *db, long long V, int C, cudaStream_t s);
+void net_mse(const float *pred, const float *target, float *dpred, long long n, double *partial,
+             unsigned *counter, double *loss, cudaStream_t s);
+void net_adam(float *w, float *wq, const float *g, float *m, float *v, long long n, float lr,
+              int step, float gscale, cudaStream_t s);
+void net_round_bf16(const float *w, float *wq, long long n, cudaStream_t s);
+void net_input(const float *i0, const float *i1, float *x, long long V, float scale,
+               cudaStream_t s);
+void net_add_into(float *a, const float *b, long long n, cudaStream_t s);
+
 }  // namespace flof
