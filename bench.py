@@ -50,7 +50,9 @@ def args_():
     ap.add_argument("--blur-type", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="flof", choices=["flof", "batch", "mixed"],
+    ap.add_argument("--train-pairs", type=int, default=256)
+    ap.add_argument("--train-epochs", type=int, default=20)
+    ap.add_argument("--workload", default="flof", choices=["flof", "batch", "mixed", "learned"],
                     help="flof: the two-way 64^4 workload (default); batch: 64 independent solves of "
                          "uneven sizes, concurrent against sequential; mixed: the 96^4 solve in mixed "
                          "precision against FP32")
@@ -535,6 +537,83 @@ def run_mixed(a):
     ctx.close()
 
 
+def net_flops(res: int) -> float:
+    """Forward FLOPs of the warm start network at coarse extent res:
+    2 * taps * cin * cout per output voxel and layer."""
+    layers = [(2, 16, 81, 1), (16, 32, 81, 2), (32, 32, 81, 2), (32, 64, 81, 4), (64, 64, 81, 4),
+              (96, 32, 81, 2), (48, 16, 81, 1), (16, 4, 1, 1)]
+    return float(sum(2 * taps * ci * co * (res // div) ** 4 for ci, co, taps, div in layers))
+
+
+def run_learned(a):
+    """The learned warm start: trained on the GPU from plain-solver outputs of
+    seeded 1-3 drop pairs at 32^4, then the two-way deformations of the
+    standard inputs at --res solved cold and warm-started."""
+    import torch
+    import ofblend_gb300 as F
+    from ofblend_gb300 import synth, warmstart
+    torch.cuda.set_device(0)
+    ctx = F.Context(0)
+    t0 = time.perf_counter()
+    samples = warmstart.make_samples(a.train_pairs, base_seed=10000,
+                                     solve_params=dict(flof_params(0.01, a.blur_type)), ctx=ctx)
+    t_data = time.perf_counter() - t0
+    m = F.Model(16, ctx=ctx, seed=1)
+    t0 = time.perf_counter()
+    hist = warmstart.train(m, samples, epochs=a.train_epochs, batch=16, lr=2e-3)
+    ctx.synchronize()
+    t_train = time.perf_counter() - t0
+    m.attach()
+    R = a.res
+    dims = (R, R, R, R)
+    s0, s1 = synth.scene_for(0), synth.scene_for(1)
+    g0 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(synth.flow_input(s0, dims))
+    g1 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(synth.flow_input(s1, dims))
+    v = F.Grid4Vec4(dims=dims, ctx=ctx)
+    p = flof_params(a.cg_accuracy, a.blur_type)
+    res = {}
+    for mode in ("plain", "warm"):
+        def step():
+            st = []
+            for x, y in ((g0, g1), (g1, g0)):
+                v.setConst(0.0)
+                F.opticalFlowMultiscale4d(v, x, y, warmStart=(mode == "warm"), **p)
+                st.append(F.last_solve_stats())
+            return st
+        for _ in range(max(a.warmup, 1)):
+            step()
+        ctx.synchronize()
+        tt = time.perf_counter()
+        for _ in range(max(a.steps, 1)):
+            st = step()
+        ctx.synchronize()
+        sec = (time.perf_counter() - tt) / max(a.steps, 1)
+        res[mode] = {"solves_per_s": round(2.0 / sec, 4), "ms_per_step": round(sec * 1e3, 2),
+                     "cg_iterations": [x["cg_total_iterations"] for x in st],
+                     "warm_start": [x["warm_start"] for x in st],
+                     "coarse_err_zero_vs_pred": [x["warm_start_err"] for x in st]}
+    fl = net_flops(16)
+    nsamp = a.train_pairs * a.train_epochs
+    line = {
+        "metric": f"4D flow solves/s at {R}^4 to fixed residual: learned warm-start vs plain CG",
+        "value": res["warm"]["solves_per_s"], "unit": UNIT, "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": res["warm"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16 weights, f32 accumulate)",
+        "data": "synthetic (training: seeded 1-3 drop pairs at 32^4; evaluation: data 0 <-> 1)",
+        "config": {"workload": f"both deformations at {R}^4, flof parameters, cgAccuracy {a.cg_accuracy}",
+                   "train_pairs": a.train_pairs, "train_epochs": a.train_epochs},
+        "plain": res["plain"], "warm": res["warm"],
+        "speedup_vs_plain": round(res["warm"]["solves_per_s"] / res["plain"]["solves_per_s"], 4),
+        "training": {"data_seconds": round(t_data, 2), "train_seconds": round(t_train, 2),
+                     "loss_first_last": [round(hist[0], 6), round(hist[-1], 6)],
+                     "samples_per_s": round(nsamp / t_train, 1),
+                     "net_tflops_fwd_bwd": round(3 * fl * nsamp / t_train / 1e12, 3)},
+    }
+    print(json.dumps(line), flush=True)
+    m.detach()
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = args_()
     if a.impl == "reference":
@@ -543,5 +622,7 @@ if __name__ == "__main__":
         run_batch(a)
     elif a.workload == "mixed":
         run_mixed(a)
+    elif a.workload == "learned":
+        run_learned(a)
     else:
         run_gpu(a)

@@ -251,8 +251,10 @@ void net_conv_fwd(const float *in, const float *w, const float *b, float *out, i
                   int cin, int cout, int ks, int stride, int relu, cudaStream_t s);
 void net_conv_bwd_data(const float *dout, const float *w, float *din, int rin, int rout,
                        int cin, int cout, int ks, int stride, cudaStream_t s);
-void net_conv_bwd_weight(const float *in, const float *dout, float *dw, int rin, int rout,
-                         int cin, int cout, int ks, int stride, cudaStream_t s);
+// dw = weight gradient; work holds net_conv_bwd_weight_work(...) floats
+size_t net_conv_bwd_weight_work(int rout, int cin, int cout, int ks);
+void net_conv_bwd_weight(const float *in, const float *dout, float *dw, float *work, int rin,
+                         int rout, int cin, int cout, int ks, int stride, cudaStream_t s);
 void net_relu_bwd(float *dy, const float *y, long long n, cudaStream_t s);
 void net_upcat(const float *lo, const float *skip, float *out, int R, int c1, int c2,
                cudaStream_t s);

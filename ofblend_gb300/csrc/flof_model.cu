@@ -44,6 +44,7 @@ struct flof_model {
   long long woff[8], boff[8], wsize[8];
   float *w = nullptr, *wq = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
   float *scratch = nullptr;  // one layer's weight gradient
+  float *work = nullptr;     // split-reduction slices of a weight gradient
   int step = 0;
   // activations and their gradients
   float *x = nullptr, *a[7] = {}, *c5 = nullptr, *c6 = nullptr, *out = nullptr;
@@ -98,7 +99,7 @@ void layer_bwd(flof_model *m, int l, const float *in, const float *dy, float *di
   const int R = m->R;
   cudaStream_t s = S(m);
   const int rin = R / L.rin_div, rout = R / L.rout_div;
-  net_conv_bwd_weight(in, dy, m->scratch, rin, rout, L.cin, L.cout, L.ks, L.stride, s);
+  net_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.ks, L.stride, s);
   net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l], s);
   net_bias_grad(dy, m->scratch, (long long)rout * rout * rout * rout, L.cout, s);
   net_add_into(m->grad + m->boff[l], m->scratch, L.cout, s);
@@ -187,6 +188,13 @@ FLOF_API int flof_model_create(flof_ctx *c, int res, flof_model **out) {
     m->m = m->alloc(off);
     m->v = m->alloc(off);
     m->scratch = m->alloc(maxw);
+    size_t maxwork = 0;
+    for (int l = 0; l < 8; ++l) {
+      const LayerDef &L = LAYERS[l];
+      const size_t wk = net_conv_bwd_weight_work(res / L.rout_div, L.cin, L.cout, L.ks);
+      maxwork = wk > maxwork ? wk : maxwork;
+    }
+    m->work = m->alloc(maxwork);
     const long long V1 = m->V(1), V2 = m->V(2), V4 = m->V(4);
     m->x = m->alloc(V1 * 2);
     const long long asz[7] = {V1 * 16, V2 * 32, V2 * 32, V4 * 64, V4 * 64, V2 * 32, V1 * 16};

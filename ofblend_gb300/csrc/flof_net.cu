@@ -32,83 +32,120 @@ struct ConvGeom {
   int taps;            // ks^4
 };
 
-// input voxel seen by output voxel v through tap `tap`, or -1 (padding)
-__device__ __forceinline__ int conv_src(const ConvGeom &g, int v, int tap) {
-  const int R = g.rout;
-  int o[4] = {v % R, (v / R) % R, (v / (R * R)) % R, v / (R * R * R)};
-  int tq = tap, s = 0;
-  int src[4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int off = tq % g.ks;
-    tq /= g.ks;
-    src[a] = o[a] * g.stride + off - g.pad;
-    if (src[a] < 0 || src[a] >= g.rin) return -1;
-  }
-  const int Ri = g.rin;
-  s = src[0] + Ri * (src[1] + Ri * (src[2] + Ri * src[3]));
-  return s;
-}
-
-// output voxel that reaches input voxel u through tap `tap`, or -1
-__device__ __forceinline__ int conv_dst(const ConvGeom &g, int u, int tap) {
-  const int Ri = g.rin;
-  int in[4] = {u % Ri, (u / Ri) % Ri, (u / (Ri * Ri)) % Ri, u / (Ri * Ri * Ri)};
-  int tq = tap;
-  int o[4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int off = tq % g.ks;
-    tq /= g.ks;
-    const int num = in[a] + g.pad - off;
-    if (num < 0) return -1;
-    if (g.stride == 2 && (num & 1)) return -1;
-    o[a] = num / g.stride;
-    if (o[a] >= g.rout) return -1;
-  }
-  const int R = g.rout;
-  return o[0] + R * (o[1] + R * (o[2] + R * o[3]));
+__device__ __forceinline__ void vox_coords(int v, int R, int c[4]) {
+  c[0] = v % R;
+  v /= R;
+  c[1] = v % R;
+  v /= R;
+  c[2] = v % R;
+  c[3] = v / R;
 }
 
 // MODE 0 forward:   C[v][co]  = sum_{tap,ci} in[src(v,tap)][ci] * W[tap][ci][co]
 // MODE 1 bwd data:  C[u][ci]  = sum_{tap,co} dout[dst(u,tap)][co] * W[tap][ci][co]
 // MODE 2 bwd weight: C[(tap,ci)][co] = sum_v in[src(v,tap)][ci] * dout[v][co]
+// src(v, tap) = v * stride + off(tap) - pad per axis (zero outside); dst is
+// its inverse.  Voxel coordinates of the tile's rows and the (tap, channel)
+// split of each reduction chunk are decoded once into shared memory.  MODE 2
+// reduces over output voxels and is split along that reduction into
+// gridDim.z slices written to C + z * M * N (summed by k_sum_slices).
 template <int MODE>
 __global__ void __launch_bounds__(GT_T)
 k_conv_gemm(const float *__restrict__ A, const float *__restrict__ Bsrc,
             const float *__restrict__ bias, float *__restrict__ C, ConvGeom g, int M, int N,
-            int K, int relu) {
+            int K, int relu, int kslice) {
   __shared__ float As[GT_K][GT_M + 4];
   __shared__ float Bs[GT_K][GT_N + 4];
+  __shared__ int rowc[GT_M][4];   // MODE 0/1: voxel coordinates of the rows
+  __shared__ int rowx[GT_M][2];   // MODE 2: (tap, ci) of the rows
+  __shared__ int kc[GT_K][5];     // MODE 0/1: (tap offsets x,y,z,t, channel); MODE 2: voxel
   const int m0 = blockIdx.x * GT_M, n0 = blockIdx.y * GT_N;
+  const int kbeg = MODE == 2 ? blockIdx.z * kslice : 0;
+  const int kend = MODE == 2 ? min(K, kbeg + kslice) : K;
   const int tid = threadIdx.x;
   const int tr = tid / 8, tc = tid % 8;  // 16 x 8 threads
+  const int ch = MODE == 0 ? g.cin : g.cout;  // channels of the reduction (MODE 0/1)
+  if (tid < GT_M) {
+    const int m = m0 + tid;
+    if (MODE == 2) {
+      rowx[tid][0] = m < M ? m / g.cin : 0;
+      rowx[tid][1] = m < M ? m % g.cin : 0;
+    } else {
+      int c[4] = {0, 0, 0, 0};
+      if (m < M) vox_coords(m, MODE == 0 ? g.rout : g.rin, c);
+#pragma unroll
+      for (int a = 0; a < 4; ++a) rowc[tid][a] = c[a];
+    }
+  }
   float acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
 
-  for (int k0 = 0; k0 < K; k0 += GT_K) {
+  for (int k0 = kbeg; k0 < kend; k0 += GT_K) {
+    if (tid < GT_K) {
+      const int k = k0 + tid;
+      if (MODE == 2) {
+        int c[4] = {0, 0, 0, 0};
+        if (k < kend) vox_coords(k, g.rout, c);
+        kc[tid][0] = c[0];
+        kc[tid][1] = c[1];
+        kc[tid][2] = c[2];
+        kc[tid][3] = c[3];
+        kc[tid][4] = k < kend ? 1 : 0;
+      } else {
+        const int tap = k < kend ? k / ch : 0;
+        kc[tid][4] = k < kend ? k % ch : -1;
+        int tq = tap;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          kc[tid][a] = tq % g.ks;
+          tq /= g.ks;
+        }
+      }
+    }
+    __syncthreads();
     // A tile: GT_M rows x GT_K reduction entries
     for (int e = tid; e < GT_M * GT_K; e += GT_T) {
       const int mm = e / GT_K, kk = e % GT_K;
-      const int m = m0 + mm, k = k0 + kk;
+      const int m = m0 + mm;
       float val = 0.f;
-      if (m < M && k < K) {
+      if (m < M && (MODE == 2 ? kc[kk][4] != 0 : kc[kk][4] >= 0)) {
         if (MODE == 0) {
-          const int tap = k / g.cin, ci = k % g.cin;
-          const int s = conv_src(g, m, tap);
-          if (s >= 0) val = __ldg(A + (size_t)s * g.cin + ci);
+          int s = 0, ok = 1, mul = 1;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int q = rowc[mm][a] * g.stride + kc[kk][a] - g.pad;
+            ok &= (q >= 0) & (q < g.rin);
+            s += q * mul;
+            mul *= g.rin;
+          }
+          if (ok) val = __ldg(A + (size_t)s * g.cin + kc[kk][4]);
         } else if (MODE == 1) {
-          const int tap = k / g.cout, co = k % g.cout;
-          const int dv = conv_dst(g, m, tap);
-          if (dv >= 0) val = __ldg(A + (size_t)dv * g.cout + co);
+          int s = 0, ok = 1, mul = 1;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int num = rowc[mm][a] + g.pad - kc[kk][a];
+            const int o = num / g.stride;
+            ok &= (num >= 0) & (o * g.stride == num) & (o < g.rout);
+            s += o * mul;
+            mul *= g.rout;
+          }
+          if (ok) val = __ldg(A + (size_t)s * g.cout + kc[kk][4]);
         } else {
-          // rows are (tap, ci), the reduction runs over output voxels v = k
-          const int tap = m / g.cin, ci = m % g.cin;
-          const int s = conv_src(g, k, tap);
-          if (s >= 0) val = __ldg(A + (size_t)s * g.cin + ci);
+          const int tap = rowx[mm][0], ci = rowx[mm][1];
+          int s = 0, ok = 1, mul = 1, tq = tap;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            const int off = tq % g.ks;
+            tq /= g.ks;
+            const int q = kc[kk][a] * g.stride + off - g.pad;
+            ok &= (q >= 0) & (q < g.rin);
+            s += q * mul;
+            mul *= g.rin;
+          }
+          if (ok) val = __ldg(A + (size_t)s * g.cin + ci);
         }
       }
       As[kk][mm] = val;
@@ -118,7 +155,7 @@ k_conv_gemm(const float *__restrict__ A, const float *__restrict__ Bsrc,
       const int kk = e / GT_N, nn = e % GT_N;
       const int k = k0 + kk, n = n0 + nn;
       float val = 0.f;
-      if (k < K && n < N) {
+      if (k < kend && n < N) {
         if (MODE == 0) {
           val = __ldg(Bsrc + (size_t)k * g.cout + n);  // W[(tap, ci)][co]
         } else if (MODE == 1) {
@@ -145,6 +182,7 @@ k_conv_gemm(const float *__restrict__ A, const float *__restrict__ Bsrc,
     }
     __syncthreads();
   }
+  float *Cz = MODE == 2 ? C + (size_t)blockIdx.z * M * N : C;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int m = m0 + tr * 4 + i;
@@ -158,8 +196,19 @@ k_conv_gemm(const float *__restrict__ A, const float *__restrict__ Bsrc,
         if (bias) v += __ldg(bias + n);
         if (relu) v = v > 0.f ? v : 0.f;
       }
-      C[(size_t)m * N + n] = v;
+      Cz[(size_t)m * N + n] = v;
     }
+  }
+}
+
+// out[i] = sum over the z slices of in (in order)
+__global__ void k_sum_slices(const float *__restrict__ in, float *__restrict__ out, long long n,
+                             int nz) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int z = 0; z < nz; ++z) s += in[(size_t)z * n + q];
+    out[q] = s;
   }
 }
 
@@ -321,7 +370,7 @@ void net_conv_fwd(const float *in, const float *w, const float *b, float *out, i
   const ConvGeom g = geom(rin, rout, cin, cout, ks, stride);
   const int M = rout * rout * rout * rout, N = cout, K = g.taps * cin;
   dim3 grid((M + GT_M - 1) / GT_M, (N + GT_N - 1) / GT_N);
-  k_conv_gemm<0><<<grid, GT_T, 0, s>>>(in, w, b, out, g, M, N, K, relu);
+  k_conv_gemm<0><<<grid, GT_T, 0, s>>>(in, w, b, out, g, M, N, K, relu, K);
 }
 
 void net_conv_bwd_data(const float *dout, const float *w, float *din, int rin, int rout,
@@ -329,15 +378,35 @@ void net_conv_bwd_data(const float *dout, const float *w, float *din, int rin, i
   const ConvGeom g = geom(rin, rout, cin, cout, ks, stride);
   const int M = rin * rin * rin * rin, N = cin, K = g.taps * cout;
   dim3 grid((M + GT_M - 1) / GT_M, (N + GT_N - 1) / GT_N);
-  k_conv_gemm<1><<<grid, GT_T, 0, s>>>(dout, w, nullptr, din, g, M, N, K, 0);
+  k_conv_gemm<1><<<grid, GT_T, 0, s>>>(dout, w, nullptr, din, g, M, N, K, 0, K);
 }
 
-void net_conv_bwd_weight(const float *in, const float *dout, float *dw, int rin, int rout,
-                         int cin, int cout, int ks, int stride, cudaStream_t s) {
+// The weight gradient reduces over all output voxels: the reduction is split
+// into slices (about four blocks per SM in total) whose partial products go
+// to `work` (slices x M x N floats) and are summed in slice order.
+size_t net_conv_bwd_weight_work(int rout, int cin, int cout, int ks) {
+  const int taps = ks == 3 ? 81 : 1;
+  const long long M = (long long)taps * cin, N = cout, K = (long long)rout * rout * rout * rout;
+  const long long tiles = ((M + GT_M - 1) / GT_M) * ((N + GT_N - 1) / GT_N);
+  long long slices = (4LL * sm_count() + tiles - 1) / tiles;
+  const long long maxs = (K + 255) / 256;
+  if (slices > maxs) slices = maxs;
+  if (slices < 1) slices = 1;
+  return (size_t)(slices * M * N);
+}
+
+void net_conv_bwd_weight(const float *in, const float *dout, float *dw, float *work, int rin,
+                         int rout, int cin, int cout, int ks, int stride, cudaStream_t s) {
   const ConvGeom g = geom(rin, rout, cin, cout, ks, stride);
   const int M = g.taps * cin, N = cout, K = rout * rout * rout * rout;
-  dim3 grid((M + GT_M - 1) / GT_M, (N + GT_N - 1) / GT_N);
-  k_conv_gemm<2><<<grid, GT_T, 0, s>>>(in, dout, nullptr, dw, g, M, N, K, 0);
+  const long long slices = (long long)net_conv_bwd_weight_work(rout, cin, cout, ks) / ((long long)M * N);
+  int kslice = (int)((K + slices - 1) / slices);
+  kslice = (kslice + GT_K - 1) / GT_K * GT_K;
+  const int nz = (K + kslice - 1) / kslice;
+  dim3 grid((M + GT_M - 1) / GT_M, (N + GT_N - 1) / GT_N, nz);
+  k_conv_gemm<2><<<grid, GT_T, 0, s>>>(in, dout, nullptr, work, g, M, N, K, 0, kslice);
+  const long long n = (long long)M * N;
+  k_sum_slices<<<grid_for(n, 256), 256, 0, s>>>(work, dw, n, nz);
 }
 
 void net_relu_bwd(float *dy, const float *y, long long n, cudaStream_t s) {
