@@ -143,12 +143,20 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    """Per-launch DRAM bytes (read + write) of the kernel classes measured by
+    ncu at 64^4, from the committed summary's table (profiles/)."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_cg_64.md")
+    out = {}
     if os.path.exists(p):
         with open(p) as f:
-            return json.load(f)
-    return {}
+            for ln in f:
+                cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+                if len(cells) >= 4 and cells[0].startswith("cg_"):
+                    try:
+                        out[cells[0]] = float(cells[3]) * 1e6
+                    except ValueError:
+                        pass
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -244,7 +252,7 @@ def roofline(records, R, peak, peak_kind, traffic):
     dom = max(per, key=lambda k: per[k][2])
     n, nb, ms = per[dom]
     achieved = (nb / n) / ((ms / n) * 1e-3) / 1e9
-    tr = traffic.get(dom)
+    tr = traffic.get(dom) if R == 64 else None  # the summary was captured at 64^4
     rl = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
           "frac": round(achieved / peak, 4), "traffic": tr, "kernel": dom,
           "launches": n, "bytes_per_launch": nb / n, "ms_per_launch": ms / n,
