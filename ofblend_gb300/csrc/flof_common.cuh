@@ -96,28 +96,38 @@ struct IW4 {
   float s0, s1, t0, t1, f0, f1, g0, g1;
 };
 
+// One axis of BUILD_INDEX_4D: base index b and the weights (w0, w1) of b and
+// b + 1 for a sample at p on an axis of n cells.
+struct AxisW {
+  int b;
+  float w0, w1;
+};
+
+__device__ __forceinline__ AxisW axis_index(float p, int n) {
+  AxisW a;
+  const float px = p - 0.5f;
+  a.b = trunc_i(px);
+  a.w1 = px - (float)a.b;
+  a.w0 = 1.0f - a.w1;
+  if (px < 0.f) { a.b = 0; a.w0 = 1.f; a.w1 = 0.f; }
+  if (a.b >= n - 1) { a.b = n - 2; a.w0 = 0.f; a.w1 = 1.f; }
+  return a;
+}
+
 __device__ __forceinline__ IW4 build_index4(const Dims4 &sz, float p0, float p1,
                                             float p2, float p3) {
   IW4 w;
-  const float px = p0 - 0.5f, py = p1 - 0.5f, pz = p2 - 0.5f, pt = p3 - 0.5f;
-  int xi = trunc_i(px), yi = trunc_i(py), zi = trunc_i(pz), ti = trunc_i(pt);
-  w.s1 = px - (float)xi;
-  w.s0 = 1.0f - w.s1;
-  w.t1 = py - (float)yi;
-  w.t0 = 1.0f - w.t1;
-  w.f1 = pz - (float)zi;
-  w.f0 = 1.0f - w.f1;
-  w.g1 = pt - (float)ti;
-  w.g0 = 1.0f - w.g1;
-  if (px < 0.f) { xi = 0; w.s0 = 1.f; w.s1 = 0.f; }
-  if (py < 0.f) { yi = 0; w.t0 = 1.f; w.t1 = 0.f; }
-  if (pz < 0.f) { zi = 0; w.f0 = 1.f; w.f1 = 0.f; }
-  if (pt < 0.f) { ti = 0; w.g0 = 1.f; w.g1 = 0.f; }
-  if (xi >= sz.x - 1) { xi = sz.x - 2; w.s0 = 0.f; w.s1 = 1.f; }
-  if (yi >= sz.y - 1) { yi = sz.y - 2; w.t0 = 0.f; w.t1 = 1.f; }
-  if (zi >= sz.z - 1) { zi = sz.z - 2; w.f0 = 0.f; w.f1 = 1.f; }
-  if (ti >= sz.t - 1) { ti = sz.t - 2; w.g0 = 0.f; w.g1 = 1.f; }
-  w.idx = sz.index(xi, yi, zi, ti);
+  const AxisW ax = axis_index(p0, sz.x), ay = axis_index(p1, sz.y);
+  const AxisW az = axis_index(p2, sz.z), at = axis_index(p3, sz.t);
+  w.s0 = ax.w0;
+  w.s1 = ax.w1;
+  w.t0 = ay.w0;
+  w.t1 = ay.w1;
+  w.f0 = az.w0;
+  w.f1 = az.w1;
+  w.g0 = at.w0;
+  w.g1 = at.w1;
+  w.idx = sz.index(ax.b, ay.b, az.b, at.b);
   return w;
 }
 

@@ -636,37 +636,81 @@ void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
 // Projection correction (optflow4d.cpp:651-734)
 // ---------------------------------------------------------------------------
 
-__device__ float4 normal_interp(const float *__restrict__ phi, const Dims4 &d, float p0,
-                                float p1, float p2, float p3) {
-  const float h = 0.5f;
-  float4 n;
-  n.x = interp4_real(phi, d, p0 + h, p1, p2, p3) - interp4_real(phi, d, p0 - h, p1, p2, p3);
-  n.y = interp4_real(phi, d, p0, p1 + h, p2, p3) - interp4_real(phi, d, p0, p1 - h, p2, p3);
-  n.z = interp4_real(phi, d, p0, p1, p2 + h, p3) - interp4_real(phi, d, p0, p1, p2 - h, p3);
-  n.w = interp4_real(phi, d, p0, p1, p2, p3 + h) - interp4_real(phi, d, p0, p1, p2, p3 - h);
-  // normalize (util/vector4d.h:331-345)
-  const float len2 = n.x * n.x + n.y * n.y + n.z * n.z + n.w * n.w;
-  const float eps2 = 1e-6f * 1e-6f;
-  if (fabs((double)len2 - 1.) < (double)eps2) {
-    // normalized enough
-  } else if (len2 > eps2) {
-    const float nrm = __fsqrt_rn(len2);
-    const float inv = __frcp_rn(nrm);
-    n.x *= inv;
-    n.y *= inv;
-    n.z *= inv;
-    n.w *= inv;
-  } else {
-    n = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  return n;
+// The projection samples phiOrg 9 times around each cell (the centre and
+// +-0.5 along each axis for the normal) and then once per search step.  The
+// samples share taps: along each axis the +-0.5 bases differ from the
+// centre's by at most one, so the 2^4 centre block plus one 8-tap face per
+// shifted sample that moved covers all nine (48 loads instead of 144 when
+// nothing is clamped).  Search steps reuse the taps while the probe stays in
+// the same cell, which is every step once the normal is zero (flat, clamped
+// regions).  The weights and the sum order are those of interp4_real, so the
+// values are the same bit for bit.
+
+// c[t*8 + z*4 + x*2 + y]: the interp4_sum order.
+__device__ __forceinline__ float ip16(const float (&c)[16], const AxisW &ax, const AxisW &ay,
+                                      const AxisW &az, const AxisW &at) {
+  const float s0 = ax.w0, s1 = ax.w1, t0 = ay.w0, t1 = ay.w1;
+  const float f0 = az.w0, f1 = az.w1, g0 = at.w0, g1 = at.w1;
+  return (((c[0] * t0 + c[1] * t1) * s0 + (c[2] * t0 + c[3] * t1) * s1) * f0 +
+          ((c[4] * t0 + c[5] * t1) * s0 + (c[6] * t0 + c[7] * t1) * s1) * f1) *
+             g0 +
+         (((c[8] * t0 + c[9] * t1) * s0 + (c[10] * t0 + c[11] * t1) * s1) * f0 +
+          ((c[12] * t0 + c[13] * t1) * s0 + (c[14] * t0 + c[15] * t1) * s1) * f1) *
+             g1;
 }
 
-__global__ void k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
-                                const float *__restrict__ phiOrg,
-                                const float *__restrict__ phiTarget, float *__restrict__ marker,
-                                Dims4 d, BoxDecoder bx, uint32_t nbox, float threshPhi,
-                                int maxIter) {
+__device__ __forceinline__ idx_t tap_off(int q, idx_t sY, idx_t sZ, idx_t sT) {
+  return (idx_t)((q >> 1) & 1) + (idx_t)(q & 1) * sY + (idx_t)((q >> 2) & 1) * sZ +
+         (idx_t)((q >> 3) & 1) * sT;
+}
+
+__device__ __forceinline__ void load_taps(const float *__restrict__ phi, idx_t i, idx_t sY,
+                                          idx_t sZ, idx_t sT, float (&c)[16]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) c[q] = __ldg(phi + i + tap_off(q, sY, sZ, sT));
+}
+
+// The sample at the centre position with axis D moved to `s`.
+template <int D>
+__device__ __forceinline__ float shifted_sample(const float *__restrict__ phi, const Dims4 &d,
+                                                const float (&C)[16], idx_t ic,
+                                                const AxisW (&a)[4], const AxisW &s, float p0,
+                                                float p1, float p2, float p3) {
+  constexpr int bit = D == 0 ? 2 : D == 1 ? 1 : D == 2 ? 4 : 8;
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  const idx_t sD = D == 0 ? 1 : D == 1 ? sY : D == 2 ? sZ : sT;
+  const int delta = s.b - a[D].b;
+  if (delta < -1 || delta > 1) return interp4_real(phi, d, p0, p1, p2, p3);
+  float S[16];
+  if (delta == 0) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) S[q] = C[q];
+  } else if (delta > 0) {
+    const idx_t f = ic + 2 * sD;
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (!(q & bit)) {
+        S[q] = C[q | bit];
+        S[q | bit] = __ldg(phi + f + tap_off(q, sY, sZ, sT));
+      }
+  } else {
+    const idx_t f = ic - sD;
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (!(q & bit)) {
+        S[q] = __ldg(phi + f + tap_off(q, sY, sZ, sT));
+        S[q | bit] = C[q];
+      }
+  }
+  return ip16(S, D == 0 ? s : a[0], D == 1 ? s : a[1], D == 2 ? s : a[2], D == 3 ? s : a[3]);
+}
+
+__global__ void __launch_bounds__(128)
+k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
+                const float *__restrict__ phiOrg, const float *__restrict__ phiTarget,
+                float *__restrict__ marker, Dims4 d, BoxDecoder bx, uint32_t nbox,
+                float threshPhi, int maxIter) {
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nbox;
        q += gridDim.x * blockDim.x) {
     int i, j, k, l;
@@ -678,25 +722,84 @@ __global__ void k_project_cells(float4 *__restrict__ dst, const float4 *__restri
     const float p1 = (float)(j + 0.5f) - v.y * dt;
     const float p2 = (float)(k + 0.5f) - v.z * dt;
     const float p3 = (float)(l + 0.5f) - v.w * dt;
-    const float4 nrm = normal_interp(phiOrg, d, p0, p1, p2, p3);
+    const AxisW a[4] = {axis_index(p0, d.x), axis_index(p1, d.y), axis_index(p2, d.z),
+                        axis_index(p3, d.t)};
+    const idx_t ic = d.index(a[0].b, a[1].b, a[2].b, a[3].b);
+    float T[16];
+    load_taps(phiOrg, ic, sY, sZ, sT, T);
+    // normal at p: central differences with h = 0.5 (optflow4d.cpp:655-661)
+    const float h = 0.5f;
+    float4 nrm;
+    nrm.x = shifted_sample<0>(phiOrg, d, T, ic, a, axis_index(p0 + h, d.x), p0 + h, p1, p2, p3) -
+            shifted_sample<0>(phiOrg, d, T, ic, a, axis_index(p0 - h, d.x), p0 - h, p1, p2, p3);
+    nrm.y = shifted_sample<1>(phiOrg, d, T, ic, a, axis_index(p1 + h, d.y), p0, p1 + h, p2, p3) -
+            shifted_sample<1>(phiOrg, d, T, ic, a, axis_index(p1 - h, d.y), p0, p1 - h, p2, p3);
+    nrm.z = shifted_sample<2>(phiOrg, d, T, ic, a, axis_index(p2 + h, d.z), p0, p1, p2 + h, p3) -
+            shifted_sample<2>(phiOrg, d, T, ic, a, axis_index(p2 - h, d.z), p0, p1, p2 - h, p3);
+    nrm.w = shifted_sample<3>(phiOrg, d, T, ic, a, axis_index(p3 + h, d.t), p0, p1, p2, p3 + h) -
+            shifted_sample<3>(phiOrg, d, T, ic, a, axis_index(p3 - h, d.t), p0, p1, p2, p3 - h);
+    // normalize (util/vector4d.h:331-345)
+    {
+      // |len2 - 1| < 1e-12 in double holds for a float len2 only at 1.0f:
+      // the floats next to 1 are 2^-24 and 2^-23 away.  The float test keeps
+      // the FP64 pipe (2 ops/clk/SM on this part) out of the kernel.
+      const float len2 = nrm.x * nrm.x + nrm.y * nrm.y + nrm.z * nrm.z + nrm.w * nrm.w;
+      const float eps2 = 1e-6f * 1e-6f;
+      if (len2 == 1.0f) {
+        // normalized enough
+      } else if (len2 > eps2) {
+        const float nl = __fsqrt_rn(len2);
+        const float inv = __frcp_rn(nl);
+        nrm.x *= inv;
+        nrm.y *= inv;
+        nrm.z *= inv;
+        nrm.w *= inv;
+      } else {
+        nrm = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
     // projectCell (optflow4d.cpp:675-710)
     float step = 0.25f;
     if (maxIter < 50) step = 0.5f;
     int lastDir = 0;
     const float targetVal = __ldg(phiTarget + id);
-    float vn = interp4_real(phiOrg, d, p0, p1, p2, p3);
+    float vn = ip16(T, a[0], a[1], a[2], a[3]);
+    idx_t ti = ic;  // T holds the taps of the cell at ti
     float dd = (vn - targetVal);
-    for (int s = 0; s < maxIter; ++s) {
+    int lim = maxIter;
+    if (nrm.x == 0.f && nrm.y == 0.f && nrm.z == 0.f && nrm.w == 0.f && isfinite(dd)) {
+      // Zero normal (flat, clamped phi): every probe is p itself (p + 0 * dd),
+      // so vn and the in-bounds test never change, the direction never flips,
+      // the step never halves and the loop runs maxIter plain steps.
+      if (maxIter > 0) {
+        if (!in_bounds(d, trunc_i(p0), trunc_i(p1), trunc_i(p2), trunc_i(p3), 0)) {
+          dd = 9999.f;
+        } else if (vn < targetVal) {
+          for (int s = 0; s < maxIter; ++s) dd += step;
+        } else {
+          for (int s = 0; s < maxIter; ++s) dd -= step;
+        }
+      }
+      lim = 0;
+    }
+    for (int s = 0; s < lim; ++s) {
       const float n0 = p0 + (nrm.x * dd) * dt;
       const float n1 = p1 + (nrm.y * dd) * dt;
       const float n2 = p2 + (nrm.z * dd) * dt;
       const float n3 = p3 + (nrm.w * dd) * dt;
       if (!in_bounds(d, trunc_i(n0), trunc_i(n1), trunc_i(n2), trunc_i(n3), 0)) {
-        s = maxIter;
+        s = lim;
         dd = 9999.f;
         continue;
       }
-      vn = interp4_real(phiOrg, d, n0, n1, n2, n3);
+      const AxisW b0 = axis_index(n0, d.x), b1 = axis_index(n1, d.y);
+      const AxisW b2 = axis_index(n2, d.z), b3 = axis_index(n3, d.t);
+      const idx_t ni = d.index(b0.b, b1.b, b2.b, b3.b);
+      if (ni != ti) {
+        load_taps(phiOrg, ni, sY, sZ, sT, T);
+        ti = ni;
+      }
+      vn = ip16(T, b0, b1, b2, b3);
       if (vn < targetVal) {
         if (lastDir < 0) step *= 0.5f;
         dd += step;
@@ -706,7 +809,9 @@ __global__ void k_project_cells(float4 *__restrict__ dst, const float4 *__restri
         dd -= step;
         lastDir = -1;
       }
-      if ((double)step < 1e-01) s = maxIter + 1;
+      // (double)step < 0.1 equals step < 0.1f for every float: 0.1f is the
+      // smallest float above 0.1.
+      if (step < 0.1f) s = lim + 1;
     }
     if (fabsf(dd) > threshPhi) {
       dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);

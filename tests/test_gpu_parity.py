@@ -173,12 +173,14 @@ def test_opticalflow4d_single_level(gpu, orc, blur, ws):
     assert rel_l2(gv.to_numpy(), want) < REL_L2_DEFO
 
 
-# the second size leaves partial tiles in x, y and t in the staged kernels
-@pytest.mark.parametrize("dims", [(20, 20, 20, 16), (37, 21, 19, 15)])
-def test_corrvelsof_bitexact(gpu, orc, dims):
+# the second size leaves partial tiles in x, y and t in the staged kernels;
+# the large velocities send samples past the borders, where the weights clamp
+@pytest.mark.parametrize("dims,vscale", [((20, 20, 20, 16), 0.8), ((37, 21, 19, 15), 0.8),
+                                         ((20, 20, 20, 16), 6.0)])
+def test_corrvelsof_bitexact(gpu, orc, dims, vscale):
     i0, i1 = drop_pair(dims)
     r = np.random.default_rng(19)
-    vel = (r.standard_normal(i0.shape + (4,)) * 0.8).astype(np.float32)
+    vel = (r.standard_normal(i0.shape + (4,)) * vscale).astype(np.float32)
     want_vel, want_dst, _ = orc.corrVelsOf4d(vel, i0, i1, 4.0, 4.0, 0.1, 40)
     gv, gd = grid_of(vel), F.Grid4Vec4(dims=dims)
     F.corrVelsOf4d(gd, gv, grid_of(i0), None, grid_of(i1), 4.0, -9.0, 4.0, 0.1, 40)
