@@ -209,8 +209,21 @@ bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const floa
 // Which cells those are comes from a packed mask that launch_expol_mask
 // builds from the marker once per round: expol_mask_words(d) 16-bit words.
 size_t expol_mask_words(Dims4 d);
-void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st);
-bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+// Zero tracking of the sweeps.  A sweep block owns one tile of cells; a tile
+// whose input neighbourhood is all zero computes +0 everywhere (sums that
+// start at +0 never give -0), so when its destination tile is already zero
+// the block has nothing to write and returns at once.  Flags per tile, 0 or
+// 1: nz_a / nz_b = some cell of the tile is nonzero in that buffer, keep_nz =
+// some cell the sweep leaves alone is nonzero.  expol_tiles(d) tiles each.
+size_t expol_tiles(Dims4 d);
+// Builds the keep-mask from the marker and the three flag arrays from the
+// projected field src (both sweep buffers hold it); the flags must be zeroed
+// first.  Flag pointers may be null (no zero tracking).
+void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
+                       uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st);
+// nz_in / nz_out: the flags of the in and out buffers (null: no skipping).
+bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
+                      uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
                       cudaStream_t st);
 
 // ---- projection correction ------------------------------------------------------
