@@ -248,9 +248,9 @@ CGTune cg_tune(flof_ctx *c, Dims4 d, const OFConsts &k) {
     CGTune cand = best;
     cand.per_sm = ps;
     const float ms = time_it([&] {
-      launch_cg_update(x.v(), r.v(), p.v(), q.v(), g.v(), d, k, st, c->dpart, c->fpart,
-                       1 << 30, c->stream, cand);
-      launch_cg_direction(p.v(), r.v(), g.v(), d, k, st, c->stream, cand);
+      launch_cg_update(r.v(), q.v(), g.v(), d, k, st, c->dpart, c->fpart, 1 << 30, c->stream,
+                       cand);
+      launch_cg_direction(x.v(), p.v(), r.v(), g.v(), d, k, st, c->stream, cand);
     });
     if (ms < bt) {
       bt = ms;
@@ -280,11 +280,10 @@ void pcg_loop(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 
     for (int s = 0; s < n; ++s) {
       KLP(c, KC_MATVEC, d.x, nint(d) * (32 + gb),
           launch_cg_matvec(p, g, q, d, k, c->st, c->dpart, c->stream, tu));
-      KLP(c, KC_UPDATE, d.x, nint(d) * (96 + gb),
-          launch_cg_update(x, r, p, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream,
-                           tu));
-      KLP(c, KC_DIRECTION, d.x, nint(d) * (48 + gb),
-          launch_cg_direction(p, r, g, d, k, c->st, c->stream, tu));
+      KLP(c, KC_UPDATE, d.x, nint(d) * (48 + gb),
+          launch_cg_update(r, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream, tu));
+      KLP(c, KC_DIRECTION, d.x, nint(d) * (80 + gb),
+          launch_cg_direction(x, p, r, g, d, k, c->st, c->stream, tu));
     }
     it += n;
     CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));

@@ -97,6 +97,7 @@ struct CGState {
   float retResidual;  // resMax / resIni
   int done;         // 0 running; see CG_* below
   int iters;
+  int xpend;        // 1: x += alpha p of the last update is still to be applied
   unsigned int counter[4];
 };
 enum { CG_RUNNING = 0, CG_CONVERGED = 1, CG_FAILED_SIGMA = 2, CG_EARLY = 3,
@@ -131,12 +132,15 @@ void launch_of_assemble_init(const float *i0w, const float *i1,
 void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
                       OFConsts c, CGState *st, double *dpart, cudaStream_t s,
                       const CGTune &tu = CGTune());
-// The update takes the iteration number from st->iters.
-void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                      const float4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+// The update (r -= alpha q, z.r, max r) takes the iteration number from
+// st->iters and leaves x += alpha p to the direction kernel, which reads p
+// anyway (st->xpend); the direction kernel applies it even after the update
+// has ended the solve.  The x values are those of the textbook order bit for
+// bit.
+void launch_cg_update(float4 *r, const float4 *q, const float4 *g, Dims4 d, OFConsts c,
+                      CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
                       const CGTune &tu = CGTune());
-void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
+void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const float4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s,
                          const CGTune &tu = CGTune());
 // The same three kernels with the image gradient stored in BF16 (mixed
@@ -144,11 +148,10 @@ void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
 void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,
                       OFConsts c, CGState *st, double *dpart, cudaStream_t s,
                       const CGTune &tu = CGTune());
-void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                      const BF4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+void launch_cg_update(float4 *r, const float4 *q, const BF4 *g, Dims4 d, OFConsts c,
+                      CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
                       const CGTune &tu = CGTune());
-void launch_cg_direction(float4 *p, const float4 *r, const BF4 *g, Dims4 d,
+void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const BF4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s,
                          const CGTune &tu = CGTune());
 // ---- mixed precision (flof_mixed.cu) ------------------------------------------

@@ -164,6 +164,7 @@ k_cg_init_r(const float4 *__restrict__ r, const BF4 *__restrict__ g, float4 *__r
       st->resIni = residual;
       st->resMax = m;
       st->iters = 0;
+      st->xpend = 0;
       st->counter[0] = 0;
       if (residual < (double)1e-6f) {
         st->retResidual = 0.f;

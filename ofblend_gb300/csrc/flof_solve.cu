@@ -131,6 +131,7 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
       st->resIni = residual;
       st->resMax = m;
       st->iters = 0;
+      st->xpend = 0;
       st->counter[0] = 0;
       if (residual < (double)1e-6f) {
         st->retResidual = 0.f;
@@ -218,6 +219,8 @@ __global__ void __launch_bounds__(MV_NT)
 k_cg_matvec(const float4 *__restrict__ p, const GT *__restrict__ g,
             float4 *__restrict__ q, Dims4 d, MVShape sh, OFConsts c, CGState *st,
             double *dpart) {
+  // the previous direction kernel has applied any pending x update
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->xpend = 0;
   if (st->done) return;
   __shared__ double shd[MV_NT / 32];
   FF dot = {0.f, 0.f};
@@ -349,11 +352,11 @@ void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,
   matvec_any(p, g, q, d, c, st, dpart, s, tu);
 }
 
-// x += alpha p; r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).
+// r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).  x += alpha p is left to
+// the direction kernel (st->xpend).
 template <class GT>
 __global__ void __launch_bounds__(NT)
-k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
-            const float4 *__restrict__ p, const float4 *__restrict__ q,
+k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
             const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
             OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
   if (st->done) return;
@@ -367,17 +370,12 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = ld_g(g, id);
-    float4 xx = x[id], rr = r[id];
-    xx.x = __fmaf_rn(a, pp.x, xx.x);
-    xx.y = __fmaf_rn(a, pp.y, xx.y);
-    xx.z = __fmaf_rn(a, pp.z, xx.z);
-    xx.w = __fmaf_rn(a, pp.w, xx.w);
+    const float4 qq = __ldg(q + id), gg = ld_g(g, id);
+    float4 rr = r[id];
     rr.x = __fmaf_rn(-a, qq.x, rr.x);
     rr.y = __fmaf_rn(-a, qq.y, rr.y);
     rr.z = __fmaf_rn(-a, qq.z, rr.z);
     rr.w = __fmaf_rn(-a, qq.w, rr.w);
-    x[id] = xx;
     r[id] = rr;
     const float4 pre = precond_of(gg, c.diag);
     ff_add(dot, (rr.x * pre.x) * rr.x);
@@ -407,6 +405,7 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
       st->resMax = m;
       st->retResidual = (float)(residual / st->resIni);
       st->iters = iter + 1;
+      st->xpend = 1;
       st->counter[2] = 0;
       if (residual <= st->acc) {
         st->done = CG_CONVERGED;
@@ -419,58 +418,88 @@ k_cg_update(float4 *__restrict__ x, float4 *__restrict__ r,
   }
 }
 
-void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                      const float4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
-                      const CGTune &tu) {
+template <class GT>
+void update_launch(float4 *r, const float4 *q, const GT *g, Dims4 d, OFConsts c, CGState *st,
+                   double *dpart, float *fpart, int maxIter, cudaStream_t s, const CGTune &tu) {
   const long long n = interior_count(d);
   k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      x, r, p, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
+      r, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
 }
-void launch_cg_update(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                      const BF4 *g, Dims4 d, OFConsts c, CGState *st,
-                      double *dpart, float *fpart, int maxIter, cudaStream_t s,
+void launch_cg_update(float4 *r, const float4 *q, const float4 *g, Dims4 d, OFConsts c,
+                      CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
                       const CGTune &tu) {
-  const long long n = interior_count(d);
-  k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      x, r, p, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
+  update_launch(r, q, g, d, c, st, dpart, fpart, maxIter, s, tu);
+}
+void launch_cg_update(float4 *r, const float4 *q, const BF4 *g, Dims4 d, OFConsts c,
+                      CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
+                      const CGTune &tu) {
+  update_launch(r, q, g, d, c, st, dpart, fpart, maxIter, s, tu);
 }
 
-// p = z + beta p
-template <class GT>
-__global__ void __launch_bounds__(NT)
-k_cg_direction(float4 *__restrict__ p, const float4 *__restrict__ r,
-               const GT *__restrict__ g, Dims4 d, BoxDecoder bx,
-               uint32_t nint, OFConsts c, CGState *st) {
-  if (st->done) return;
-  const float b = (float)st->beta;
+// x += alpha p (the last update's, when pending); then, while the solve
+// runs, p = z + beta p.
+template <bool XP, bool PN, class GT>
+__device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *__restrict__ p,
+                                                const float4 *__restrict__ r,
+                                                const GT *__restrict__ g, const Dims4 &d,
+                                                const BoxDecoder &bx, uint32_t nint,
+                                                const OFConsts &c, float a, float b) {
   for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
        n += gridDim.x * blockDim.x) {
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    const float4 rr = __ldg(r + id), gg = ld_g(g, id);
     float4 pp = p[id];
-    const float4 pre = precond_of(gg, c.diag);
-    pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
-    pp.y = __fmaf_rn(b, pp.y, rr.y * pre.y);
-    pp.z = __fmaf_rn(b, pp.z, rr.z * pre.z);
-    pp.w = __fmaf_rn(b, pp.w, rr.w * pre.w);
-    p[id] = pp;
+    if (XP) {
+      float4 xx = x[id];
+      xx.x = __fmaf_rn(a, pp.x, xx.x);
+      xx.y = __fmaf_rn(a, pp.y, xx.y);
+      xx.z = __fmaf_rn(a, pp.z, xx.z);
+      xx.w = __fmaf_rn(a, pp.w, xx.w);
+      x[id] = xx;
+    }
+    if (PN) {
+      const float4 rr = __ldg(r + id), gg = ld_g(g, id);
+      const float4 pre = precond_of(gg, c.diag);
+      pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
+      pp.y = __fmaf_rn(b, pp.y, rr.y * pre.y);
+      pp.z = __fmaf_rn(b, pp.z, rr.z * pre.z);
+      pp.w = __fmaf_rn(b, pp.w, rr.w * pre.w);
+      p[id] = pp;
+    }
   }
 }
 
-void launch_cg_direction(float4 *p, const float4 *r, const float4 *g, Dims4 d,
-                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
-  const long long n = interior_count(d);
-  k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+template <class GT>
+__global__ void __launch_bounds__(NT)
+k_cg_direction(float4 *__restrict__ x, float4 *__restrict__ p, const float4 *__restrict__ r,
+               const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c,
+               CGState *st) {
+  // st is read-only here: the update wrote it, the next matvec clears xpend
+  const bool xp = st->xpend != 0, run = st->done == 0;
+  const float a = (float)st->alpha, b = (float)st->beta;
+  if (xp && run)
+    direction_cells<true, true>(x, p, r, g, d, bx, nint, c, a, b);
+  else if (xp)
+    direction_cells<true, false>(x, p, r, g, d, bx, nint, c, a, b);
+  else if (run)
+    direction_cells<false, true>(x, p, r, g, d, bx, nint, c, a, b);
 }
-void launch_cg_direction(float4 *p, const float4 *r, const BF4 *g, Dims4 d,
-                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
+
+template <class GT>
+void direction_launch(float4 *x, float4 *p, const float4 *r, const GT *g, Dims4 d, OFConsts c,
+                      CGState *st, cudaStream_t s, const CGTune &tu) {
   const long long n = interior_count(d);
   k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+      x, p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+}
+void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const float4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
+  direction_launch(x, p, r, g, d, c, st, s, tu);
+}
+void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const BF4 *g, Dims4 d,
+                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
+  direction_launch(x, p, r, g, d, c, st, s, tu);
 }
 
 // vel = x / mDx (optflow4d.cpp:520-529); a NaN residual resets the result to
