@@ -296,6 +296,24 @@ __device__ __forceinline__ float4 ld_g(const BF4 *__restrict__ g, idx_t i) {
   return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
                      __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
 }
+// The same split in two: g_raw loads the stored value, g_value widens it.
+__device__ __forceinline__ float4 g_raw(const float4 *__restrict__ g, idx_t i) {
+  return __ldg(g + i);
+}
+__device__ __forceinline__ BF4 g_raw(const BF4 *__restrict__ g, idx_t i) {
+  const uint2 u = __ldg((const uint2 *)(g + i));
+  BF4 b;
+  b.x = (unsigned short)(u.x & 0xffffu);
+  b.y = (unsigned short)(u.x >> 16);
+  b.z = (unsigned short)(u.y & 0xffffu);
+  b.w = (unsigned short)(u.y >> 16);
+  return b;
+}
+__device__ __forceinline__ float4 g_value(const float4 &v) { return v; }
+__device__ __forceinline__ float4 g_value(const BF4 &b) {
+  return make_float4(__uint_as_float((uint32_t)b.x << 16), __uint_as_float((uint32_t)b.y << 16),
+                     __uint_as_float((uint32_t)b.z << 16), __uint_as_float((uint32_t)b.w << 16));
+}
 
 // ---- compensated accumulation ------------------------------------------------
 
@@ -315,6 +333,25 @@ __device__ __forceinline__ void ff_add(FF &a, float p) {
   a.lo += e;
 }
 __device__ __forceinline__ double ff_value(const FF &a) { return (double)a.hi + (double)a.lo; }
+// a + b in float-float: TwoSum of the high parts, then a renormalising
+// Fast2Sum (Dekker 1971).
+__device__ __forceinline__ FF ff_plus(const FF &a, const FF &b) {
+  const float s = a.hi + b.hi;
+  const float bp = s - a.hi;
+  const float e = (a.hi - (s - bp)) + (b.hi - bp);
+  const float lo = (a.lo + b.lo) + e;
+  const float hi = s + lo;
+  return {hi, lo - (hi - s)};
+}
+__device__ __forceinline__ FF warp_sum_ff(FF v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    FF b;
+    b.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
+    b.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
+    v = ff_plus(v, b);
+  }
+  return v;
+}
 
 // (float)((double)v * (1./81.)) as the reference computes it
 // (knCvExpolBlur4d, optflow4d.cpp:625), mostly without FP64 work.  With
@@ -341,6 +378,18 @@ __device__ __forceinline__ float mul_inv81(float v) {
     return f;
   }
   return (float)((double)v * c);
+}
+
+// ---- programmatic dependent launch (griddepcontrol, sm_90 and later) -------
+// pdl_wait returns once the grid this one depends on has completed and its
+// writes are visible (at once for a grid launched without the attribute);
+// pdl_launch_dependents lets the next grid of the stream be scheduled, whose
+// blocks then wait in their own pdl_wait.  The next grid launches only after
+// every block of this one has started or exited, so its waiting blocks never
+// hold back this grid's.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // ---- reductions -----------------------------------------------------------
@@ -371,6 +420,24 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
   }
   __syncthreads();
   return v;
+}
+// Block sum of float-float values on the FP32 pipe (this part issues FP64
+// at about 2 lanes per clock per SM); the result, as a double, is valid in
+// thread 0.  sh holds NT / 32 entries.
+template <int NT>
+__device__ __forceinline__ double block_sum_ff(FF v, FF *sh) {
+  v = warp_sum_ff(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    v = (l < NT / 32) ? sh[l] : FF{0.f, 0.f};
+    v = warp_sum_ff(v);
+    if (l == 0) r = ff_value(v);
+  }
+  __syncthreads();
+  return r;
 }
 template <int NT>
 __device__ __forceinline__ float block_max(float v, float *sh) {

@@ -93,6 +93,8 @@ struct CGState {
   double acc;       // accuracy * max(r0)
   double resIni;    // max(r0)
   double pAp;
+  float alphaf;     // (float)alpha and (float)beta, the values the kernels use
+  float betaf;
   float resMax;     // max(r) after the last update
   float retResidual;  // resMax / resIni
   int done;         // 0 running; see CG_* below

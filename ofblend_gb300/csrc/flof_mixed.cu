@@ -122,6 +122,7 @@ k_cg_init_r(const float4 *__restrict__ r, const BF4 *__restrict__ g, float4 *__r
             Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c, float accuracy, CGState *st,
             double *dpart, float *fpart) {
   __shared__ double shd[NT / 32];
+  __shared__ FF shff[NT / 32];
   __shared__ float shf[NT / 32];
   FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
@@ -144,7 +145,7 @@ k_cg_init_r(const float4 *__restrict__ r, const BF4 *__restrict__ g, float4 *__r
     ff_add(dot, z.w * rr.w);
     mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
   }
-  const double bd = block_sum<NT>(ff_value(dot), shd);
+  const double bd = block_sum_ff<NT>(dot, shff);
   const float bm = block_max<NT>(mx, shf);
   if (threadIdx.x == 0) {
     dpart[blockIdx.x] = bd;

@@ -15,6 +15,32 @@
 
 namespace flof {
 
+namespace {
+// Launches a PCG kernel with programmatic stream serialisation, so that its
+// blocks are scheduled while the previous kernel drains (the kernel starts
+// with pdl_wait).  Falls back to an ordinary launch if the attribute is
+// refused.
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k, args...) != cudaSuccess) {
+    cudaGetLastError();
+    k<<<grid, block, 0, s>>>(args...);
+  }
+}
+}  // namespace
+
+
 constexpr int NT = 256;
 
 // ---------------------------------------------------------------------------
@@ -54,6 +80,7 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
                    OFConsts c, float accuracy, CGState *st, double *dpart,
                    float *fpart) {
   __shared__ double shd[NT / 32];
+  __shared__ FF shff[NT / 32];
   __shared__ float shf[NT / 32];
   FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
@@ -111,7 +138,7 @@ k_of_assemble_init(const float *__restrict__ i0w, const float *__restrict__ i1,
     ff_add(dot, z.w * rr.w);
     mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
   }
-  const double bd = block_sum<NT>(ff_value(dot), shd);
+  const double bd = block_sum_ff<NT>(dot, shff);
   const float bm = block_max<NT>(mx, shf);
   if (threadIdx.x == 0) {
     dpart[blockIdx.x] = bd;
@@ -219,10 +246,13 @@ __global__ void __launch_bounds__(MV_NT)
 k_cg_matvec(const float4 *__restrict__ p, const GT *__restrict__ g,
             float4 *__restrict__ q, Dims4 d, MVShape sh, OFConsts c, CGState *st,
             double *dpart) {
+  pdl_wait();
+  pdl_launch_dependents();
   // the previous direction kernel has applied any pending x update
   if (blockIdx.x == 0 && threadIdx.x == 0) st->xpend = 0;
   if (st->done) return;
   __shared__ double shd[MV_NT / 32];
+  __shared__ FF shff[MV_NT / 32];
   FF dot = {0.f, 0.f};
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   const float o = c.offd;
@@ -278,7 +308,7 @@ k_cg_matvec(const float4 *__restrict__ p, const GT *__restrict__ g,
       cur = nxt;
     }
   }
-  const double bd = block_sum<MV_NT>(ff_value(dot), shd);
+  const double bd = block_sum_ff<MV_NT>(dot, shff);
   if (threadIdx.x == 0) dpart[blockIdx.x] = bd;
   if (last_block_arrives(&st->counter[1])) {
     double s = 0.0;
@@ -287,6 +317,7 @@ k_cg_matvec(const float4 *__restrict__ p, const GT *__restrict__ g,
     if (threadIdx.x == 0) {
       st->pAp = s;
       st->alpha = st->sigma / s;
+      st->alphaf = (float)st->alpha;
       st->counter[1] = 0;
     }
   }
@@ -316,7 +347,7 @@ void matvec_variant(const float4 *p, const GT *g, float4 *q, Dims4 d, OFConsts c
   }();
   int blocks = sm_count() * per_sm;
   if (blocks > sh.items) blocks = sh.items > 0 ? sh.items : 1;
-  k_cg_matvec<OFFD, TT, GT><<<blocks, MV_NT, 0, s>>>(p, g, q, d, sh, c, st, dpart);
+  launch_pdl(k_cg_matvec<OFFD, TT, GT>, blocks, MV_NT, s, p, g, q, d, sh, c, st, dpart);
 }
 
 template <bool OFFD, class GT>
@@ -359,32 +390,51 @@ __global__ void __launch_bounds__(NT)
 k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
             const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
             OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (st->done) return;
   __shared__ double shd[NT / 32];
+  __shared__ FF shff[NT / 32];
   __shared__ float shf[NT / 32];
-  const float a = (float)st->alpha;
+  const float a = st->alphaf;
   FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
-       n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    const float4 qq = __ldg(q + id), gg = ld_g(g, id);
-    float4 rr = r[id];
+  auto cell = [&](idx_t id, float4 qq, GT gv, float4 rr) {
     rr.x = __fmaf_rn(-a, qq.x, rr.x);
     rr.y = __fmaf_rn(-a, qq.y, rr.y);
     rr.z = __fmaf_rn(-a, qq.z, rr.z);
     rr.w = __fmaf_rn(-a, qq.w, rr.w);
     r[id] = rr;
-    const float4 pre = precond_of(gg, c.diag);
+    const float4 pre = precond_of(g_value(gv), c.diag);
     ff_add(dot, (rr.x * pre.x) * rr.x);
     ff_add(dot, (rr.y * pre.y) * rr.y);
     ff_add(dot, (rr.z * pre.z) * rr.z);
     ff_add(dot, (rr.w * pre.w) * rr.w);
     mx = fmaxf(mx, fmaxf(fmaxf(rr.x, rr.y), fmaxf(rr.z, rr.w)));
+  };
+  // two cells per trip with all loads issued first (the thread's cell order,
+  // and so the sum order, is that of the plain grid-stride loop)
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; n + stride < nint; n += 2 * stride) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t i0 = d.index(i, j, k, l);
+    bx.decode(n + stride, i, j, k, l);
+    const idx_t i1 = d.index(i, j, k, l);
+    const float4 q0 = __ldg(q + i0), q1 = __ldg(q + i1);
+    const GT g0 = g_raw(g, i0), g1 = g_raw(g, i1);
+    const float4 r0 = r[i0], r1 = r[i1];
+    cell(i0, q0, g0, r0);
+    cell(i1, q1, g1, r1);
   }
-  const double bd = block_sum<NT>(ff_value(dot), shd);
+  if (n < nint) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t i0 = d.index(i, j, k, l);
+    cell(i0, __ldg(q + i0), g_raw(g, i0), r[i0]);
+  }
+  const double bd = block_sum_ff<NT>(dot, shff);
   const float bm = block_max<NT>(mx, shf);
   if (threadIdx.x == 0) {
     dpart[blockIdx.x] = bd;
@@ -411,6 +461,7 @@ k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
         st->done = CG_CONVERGED;
       } else {
         st->beta = s / st->sigma;
+        st->betaf = (float)st->beta;
         st->sigma = s;
         if (iter + 1 >= maxIter) st->done = CG_MAXITER;
       }
@@ -418,12 +469,26 @@ k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
   }
 }
 
+// Blocks per SM for a grid-stride PCG kernel: the tuned count, capped at what
+// fits at once, so that the grid is a single wave.
+template <class K>
+int resident_per_sm(K kernel, int want) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, NT, 0) != cudaSuccess) {
+    cudaGetLastError();
+    n = 1;
+  }
+  if (n < 1) n = 1;
+  return want < n ? want : n;
+}
+
 template <class GT>
 void update_launch(float4 *r, const float4 *q, const GT *g, Dims4 d, OFConsts c, CGState *st,
                    double *dpart, float *fpart, int maxIter, cudaStream_t s, const CGTune &tu) {
+  static const int occ = resident_per_sm(k_cg_update<GT>, 1 << 30);
   const long long n = interior_count(d);
-  k_cg_update<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      r, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
+  launch_pdl(k_cg_update<GT>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
+             NT, s, r, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
 }
 void launch_cg_update(float4 *r, const float4 *q, const float4 *g, Dims4 d, OFConsts c,
                       CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
@@ -444,14 +509,24 @@ __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *
                                                 const GT *__restrict__ g, const Dims4 &d,
                                                 const BoxDecoder &bx, uint32_t nint,
                                                 const OFConsts &c, float a, float b) {
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint;
-       n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    float4 pp = p[id];
+  struct In {
+    float4 p, x, r;
+    GT g;
+  };
+  auto load = [&](idx_t id) {
+    In v;
+    v.p = p[id];
+    if (XP) v.x = x[id];
+    if (PN) {
+      v.r = __ldg(r + id);
+      v.g = g_raw(g, id);
+    }
+    return v;
+  };
+  auto cell = [&](idx_t id, const In &v) {
+    float4 pp = v.p;
     if (XP) {
-      float4 xx = x[id];
+      float4 xx = v.x;
       xx.x = __fmaf_rn(a, pp.x, xx.x);
       xx.y = __fmaf_rn(a, pp.y, xx.y);
       xx.z = __fmaf_rn(a, pp.z, xx.z);
@@ -459,14 +534,33 @@ __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *
       x[id] = xx;
     }
     if (PN) {
-      const float4 rr = __ldg(r + id), gg = ld_g(g, id);
-      const float4 pre = precond_of(gg, c.diag);
+      const float4 rr = v.r;
+      const float4 pre = precond_of(g_value(v.g), c.diag);
       pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
       pp.y = __fmaf_rn(b, pp.y, rr.y * pre.y);
       pp.z = __fmaf_rn(b, pp.z, rr.z * pre.z);
       pp.w = __fmaf_rn(b, pp.w, rr.w * pre.w);
       p[id] = pp;
     }
+  };
+  // two cells per trip with all loads issued first
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t n = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; n + stride < nint; n += 2 * stride) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t i0 = d.index(i, j, k, l);
+    bx.decode(n + stride, i, j, k, l);
+    const idx_t i1 = d.index(i, j, k, l);
+    const In v0 = load(i0), v1 = load(i1);
+    cell(i0, v0);
+    cell(i1, v1);
+  }
+  if (n < nint) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t i0 = d.index(i, j, k, l);
+    cell(i0, load(i0));
   }
 }
 
@@ -475,9 +569,11 @@ __global__ void __launch_bounds__(NT)
 k_cg_direction(float4 *__restrict__ x, float4 *__restrict__ p, const float4 *__restrict__ r,
                const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c,
                CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   // st is read-only here: the update wrote it, the next matvec clears xpend
   const bool xp = st->xpend != 0, run = st->done == 0;
-  const float a = (float)st->alpha, b = (float)st->beta;
+  const float a = st->alphaf, b = st->betaf;
   if (xp && run)
     direction_cells<true, true>(x, p, r, g, d, bx, nint, c, a, b);
   else if (xp)
@@ -489,9 +585,10 @@ k_cg_direction(float4 *__restrict__ x, float4 *__restrict__ p, const float4 *__r
 template <class GT>
 void direction_launch(float4 *x, float4 *p, const float4 *r, const GT *g, Dims4 d, OFConsts c,
                       CGState *st, cudaStream_t s, const CGTune &tu) {
+  static const int occ = resident_per_sm(k_cg_direction<GT>, 1 << 30);
   const long long n = interior_count(d);
-  k_cg_direction<<<grid_for(n > 0 ? n : 1, NT, tu.per_sm), NT, 0, s>>>(
-      x, p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+  launch_pdl(k_cg_direction<GT>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
+             NT, s, x, p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
 }
 void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const float4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
