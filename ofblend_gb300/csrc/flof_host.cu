@@ -269,10 +269,30 @@ CGTune cg_tune(flof_ctx *c, Dims4 d, const OFConsts &k) {
 // waiting; every kernel returns at once when the state says done.  After each
 // chunk the host reads the state (into c->st_h) and sizes the next chunk from
 // the observed reduction rate.
+void pcg_update(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *r,
+                const float4 *q, const float4 *g, const float *i1, int maxIter) {
+  launch_cg_update(r, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream, tu, i1);
+}
+void pcg_update(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *r,
+                const float4 *q, const BF4 *g, const float *, int maxIter) {
+  launch_cg_update(r, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream, tu);
+}
+void pcg_direction(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *x,
+                   float4 *p, const float4 *r, const float4 *g, const float *i1) {
+  launch_cg_direction(x, p, r, g, d, k, c->st, c->stream, tu, i1);
+}
+void pcg_direction(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *x,
+                   float4 *p, const float4 *r, const BF4 *g, const float *) {
+  launch_cg_direction(x, p, r, g, d, k, c->st, c->stream, tu);
+}
+
+// i1: the FP32 solve's target level set; the update and direction kernels
+// rebuild the preconditioner's gradient from it (null: they read g).
 template <class GT>
 void pcg_loop(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 *x, float4 *r,
-              float4 *p, float4 *q, const GT *g, int maxIter) {
+              float4 *p, float4 *q, const GT *g, int maxIter, const float *i1 = nullptr) {
   const double gb = sizeof(GT) == 8 ? 8.0 : 16.0;  // bytes of g per cell
+  const double gpc = i1 ? 4.0 : gb;                 // bytes of g or i1 per cell in update/direction
   int it = 0;
   int chunk = 4;
   for (;;) {
@@ -280,10 +300,9 @@ void pcg_loop(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 
     for (int s = 0; s < n; ++s) {
       KLP(c, KC_MATVEC, d.x, nint(d) * (32 + gb),
           launch_cg_matvec(p, g, q, d, k, c->st, c->dpart, c->stream, tu));
-      KLP(c, KC_UPDATE, d.x, nint(d) * (48 + gb),
-          launch_cg_update(r, q, g, d, k, c->st, c->dpart, c->fpart, maxIter, c->stream, tu));
-      KLP(c, KC_DIRECTION, d.x, nint(d) * (80 + gb),
-          launch_cg_direction(x, p, r, g, d, k, c->st, c->stream, tu));
+      KLP(c, KC_UPDATE, d.x, nint(d) * (48 + gpc),
+          pcg_update(c, d, k, tu, r, q, g, i1, maxIter));
+      KLP(c, KC_DIRECTION, d.x, nint(d) * (80 + gpc), pcg_direction(c, d, k, tu, x, p, r, g, i1));
     }
     it += n;
     CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
@@ -390,7 +409,7 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
   if (a.precision != FLOF_PRECISION_MIXED) {
-    pcg_loop(c, d, k, tu, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter);
+    pcg_loop(c, d, k, tu, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter, i1);
     int status = c->st_h->done;
     if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
     const int iters = c->st_h->iters;

@@ -139,12 +139,14 @@ void launch_cg_matvec(const float4 *p, const float4 *g, float4 *q, Dims4 d,
 // anyway (st->xpend); the direction kernel applies it even after the update
 // has ended the solve.  The x values are those of the textbook order bit for
 // bit.
+// With i1 (the level's target level set, from which the assembly built g)
+// the two kernels rebuild g from it instead of reading g.
 void launch_cg_update(float4 *r, const float4 *q, const float4 *g, Dims4 d, OFConsts c,
                       CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
-                      const CGTune &tu = CGTune());
+                      const CGTune &tu = CGTune(), const float *i1 = nullptr);
 void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const float4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s,
-                         const CGTune &tu = CGTune());
+                         const CGTune &tu = CGTune(), const float *i1 = nullptr);
 // The same three kernels with the image gradient stored in BF16 (mixed
 // precision: the matrix g g^T + diag I is built from the rounded gradient).
 void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,

@@ -383,13 +383,34 @@ void launch_cg_matvec(const float4 *p, const BF4 *g, float4 *q, Dims4 d,
   matvec_any(p, g, q, d, c, st, dpart, s, tu);
 }
 
+// Where the update and direction kernels take the image gradient g for the
+// Jacobi preconditioner from: the stored g (FP32 or BF16), or g rebuilt from
+// the target level set i1 with the assembly's own operations (central
+// differences times 1/(2 mDx), the same values bit for bit).  i1 is 4 bytes
+// per cell against 16 for g; its neighbour loads hit L1 and L2.
+template <class T>
+struct GradStored {
+  const T *__restrict__ g;
+  __device__ __forceinline__ float4 operator()(idx_t id) const { return ld_g(g, id); }
+};
+struct GradFromI1 {
+  const float *__restrict__ i1;
+  idx_t sY, sZ, sT;
+  float dxf;
+  __device__ __forceinline__ float4 operator()(idx_t id) const {
+    return make_float4((__ldg(i1 + id + 1) - __ldg(i1 + id - 1)) * dxf,
+                       (__ldg(i1 + id + sY) - __ldg(i1 + id - sY)) * dxf,
+                       (__ldg(i1 + id + sZ) - __ldg(i1 + id - sZ)) * dxf,
+                       (__ldg(i1 + id + sT) - __ldg(i1 + id - sT)) * dxf);
+  }
+};
+
 // r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).  x += alpha p is left to
 // the direction kernel (st->xpend).
-template <class GT>
+template <class GS>
 __global__ void __launch_bounds__(NT)
-k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
-            const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint,
-            OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
+k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q, GS gs, Dims4 d, BoxDecoder bx,
+            uint32_t nint, OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter) {
   pdl_wait();
   pdl_launch_dependents();
   if (st->done) return;
@@ -399,13 +420,13 @@ k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
   const float a = st->alphaf;
   FF dot = {0.f, 0.f};
   float mx = -FLT_MAX;
-  auto cell = [&](idx_t id, float4 qq, GT gv, float4 rr) {
+  auto cell = [&](idx_t id, float4 qq, float4 gv, float4 rr) {
     rr.x = __fmaf_rn(-a, qq.x, rr.x);
     rr.y = __fmaf_rn(-a, qq.y, rr.y);
     rr.z = __fmaf_rn(-a, qq.z, rr.z);
     rr.w = __fmaf_rn(-a, qq.w, rr.w);
     r[id] = rr;
-    const float4 pre = precond_of(g_value(gv), c.diag);
+    const float4 pre = precond_of(gv, c.diag);
     ff_add(dot, (rr.x * pre.x) * rr.x);
     ff_add(dot, (rr.y * pre.y) * rr.y);
     ff_add(dot, (rr.z * pre.z) * rr.z);
@@ -423,7 +444,7 @@ k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
     bx.decode(n + stride, i, j, k, l);
     const idx_t i1 = d.index(i, j, k, l);
     const float4 q0 = __ldg(q + i0), q1 = __ldg(q + i1);
-    const GT g0 = g_raw(g, i0), g1 = g_raw(g, i1);
+    const float4 g0 = gs(i0), g1 = gs(i1);
     const float4 r0 = r[i0], r1 = r[i1];
     cell(i0, q0, g0, r0);
     cell(i1, q1, g1, r1);
@@ -432,7 +453,7 @@ k_cg_update(float4 *__restrict__ r, const float4 *__restrict__ q,
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t i0 = d.index(i, j, k, l);
-    cell(i0, __ldg(q + i0), g_raw(g, i0), r[i0]);
+    cell(i0, __ldg(q + i0), gs(i0), r[i0]);
   }
   const double bd = block_sum_ff<NT>(dot, shff);
   const float bm = block_max<NT>(mx, shf);
@@ -482,36 +503,39 @@ int resident_per_sm(K kernel, int want) {
   return want < n ? want : n;
 }
 
-template <class GT>
-void update_launch(float4 *r, const float4 *q, const GT *g, Dims4 d, OFConsts c, CGState *st,
+template <class GS>
+void update_launch(float4 *r, const float4 *q, GS gs, Dims4 d, OFConsts c, CGState *st,
                    double *dpart, float *fpart, int maxIter, cudaStream_t s, const CGTune &tu) {
-  static const int occ = resident_per_sm(k_cg_update<GT>, 1 << 30);
+  static const int occ = resident_per_sm(k_cg_update<GS>, 1 << 30);
   const long long n = interior_count(d);
-  launch_pdl(k_cg_update<GT>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
-             NT, s, r, q, g, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
+  launch_pdl(k_cg_update<GS>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
+             NT, s, r, q, gs, d, interior_decoder(d), (uint32_t)n, c, st, dpart, fpart, maxIter);
 }
 void launch_cg_update(float4 *r, const float4 *q, const float4 *g, Dims4 d, OFConsts c,
                       CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
-                      const CGTune &tu) {
-  update_launch(r, q, g, d, c, st, dpart, fpart, maxIter, s, tu);
+                      const CGTune &tu, const float *i1) {
+  if (i1)
+    update_launch(r, q, GradFromI1{i1, d.x, d.sz(), d.st(), c.dxf}, d, c, st, dpart, fpart,
+                  maxIter, s, tu);
+  else
+    update_launch(r, q, GradStored<float4>{g}, d, c, st, dpart, fpart, maxIter, s, tu);
 }
 void launch_cg_update(float4 *r, const float4 *q, const BF4 *g, Dims4 d, OFConsts c,
                       CGState *st, double *dpart, float *fpart, int maxIter, cudaStream_t s,
                       const CGTune &tu) {
-  update_launch(r, q, g, d, c, st, dpart, fpart, maxIter, s, tu);
+  update_launch(r, q, GradStored<BF4>{g}, d, c, st, dpart, fpart, maxIter, s, tu);
 }
 
 // x += alpha p (the last update's, when pending); then, while the solve
 // runs, p = z + beta p.
-template <bool XP, bool PN, class GT>
+template <bool XP, bool PN, class GS>
 __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *__restrict__ p,
-                                                const float4 *__restrict__ r,
-                                                const GT *__restrict__ g, const Dims4 &d,
-                                                const BoxDecoder &bx, uint32_t nint,
-                                                const OFConsts &c, float a, float b) {
+                                                const float4 *__restrict__ r, const GS &gs,
+                                                const Dims4 &d, const BoxDecoder &bx,
+                                                uint32_t nint, const OFConsts &c, float a,
+                                                float b) {
   struct In {
-    float4 p, x, r;
-    GT g;
+    float4 p, x, r, g;
   };
   auto load = [&](idx_t id) {
     In v;
@@ -519,7 +543,7 @@ __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *
     if (XP) v.x = x[id];
     if (PN) {
       v.r = __ldg(r + id);
-      v.g = g_raw(g, id);
+      v.g = gs(id);
     }
     return v;
   };
@@ -535,7 +559,7 @@ __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *
     }
     if (PN) {
       const float4 rr = v.r;
-      const float4 pre = precond_of(g_value(v.g), c.diag);
+      const float4 pre = precond_of(v.g, c.diag);
       pp.x = __fmaf_rn(b, pp.x, rr.x * pre.x);
       pp.y = __fmaf_rn(b, pp.y, rr.y * pre.y);
       pp.z = __fmaf_rn(b, pp.z, rr.z * pre.z);
@@ -564,39 +588,42 @@ __device__ __forceinline__ void direction_cells(float4 *__restrict__ x, float4 *
   }
 }
 
-template <class GT>
+template <class GS>
 __global__ void __launch_bounds__(NT)
 k_cg_direction(float4 *__restrict__ x, float4 *__restrict__ p, const float4 *__restrict__ r,
-               const GT *__restrict__ g, Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c,
-               CGState *st) {
+               GS gs, Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c, CGState *st) {
   pdl_wait();
   pdl_launch_dependents();
   // st is read-only here: the update wrote it, the next matvec clears xpend
   const bool xp = st->xpend != 0, run = st->done == 0;
   const float a = st->alphaf, b = st->betaf;
   if (xp && run)
-    direction_cells<true, true>(x, p, r, g, d, bx, nint, c, a, b);
+    direction_cells<true, true>(x, p, r, gs, d, bx, nint, c, a, b);
   else if (xp)
-    direction_cells<true, false>(x, p, r, g, d, bx, nint, c, a, b);
+    direction_cells<true, false>(x, p, r, gs, d, bx, nint, c, a, b);
   else if (run)
-    direction_cells<false, true>(x, p, r, g, d, bx, nint, c, a, b);
+    direction_cells<false, true>(x, p, r, gs, d, bx, nint, c, a, b);
 }
 
-template <class GT>
-void direction_launch(float4 *x, float4 *p, const float4 *r, const GT *g, Dims4 d, OFConsts c,
+template <class GS>
+void direction_launch(float4 *x, float4 *p, const float4 *r, GS gs, Dims4 d, OFConsts c,
                       CGState *st, cudaStream_t s, const CGTune &tu) {
-  static const int occ = resident_per_sm(k_cg_direction<GT>, 1 << 30);
+  static const int occ = resident_per_sm(k_cg_direction<GS>, 1 << 30);
   const long long n = interior_count(d);
-  launch_pdl(k_cg_direction<GT>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
-             NT, s, x, p, r, g, d, interior_decoder(d), (uint32_t)n, c, st);
+  launch_pdl(k_cg_direction<GS>, grid_for(n > 0 ? n : 1, NT, tu.per_sm < occ ? tu.per_sm : occ),
+             NT, s, x, p, r, gs, d, interior_decoder(d), (uint32_t)n, c, st);
 }
 void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const float4 *g, Dims4 d,
-                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
-  direction_launch(x, p, r, g, d, c, st, s, tu);
+                         OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu,
+                         const float *i1) {
+  if (i1)
+    direction_launch(x, p, r, GradFromI1{i1, d.x, d.sz(), d.st(), c.dxf}, d, c, st, s, tu);
+  else
+    direction_launch(x, p, r, GradStored<float4>{g}, d, c, st, s, tu);
 }
 void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const BF4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s, const CGTune &tu) {
-  direction_launch(x, p, r, g, d, c, st, s, tu);
+  direction_launch(x, p, r, GradStored<BF4>{g}, d, c, st, s, tu);
 }
 
 // vel = x / mDx (optflow4d.cpp:520-529); a NaN residual resets the result to
