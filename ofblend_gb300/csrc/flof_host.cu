@@ -127,7 +127,12 @@ const float *wsum_table(flof_ctx *c, float sigma, int s, const float *wtab) {
         }
   float *dptr = nullptr;
   CK(cudaMalloc(&dptr, h.size() * sizeof(float)));
-  CK(cudaMemcpy(dptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // On the context's stream and waited for: a plain cudaMemcpy from pageable
+  // memory runs on the legacy stream and may return before the data lands,
+  // and the context's non-blocking stream is not ordered after it.
+  CK(cudaMemcpyAsync(dptr, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
   c->wsum_cache[key] = dptr;
   return dptr;
 }
@@ -441,8 +446,10 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
                   float resetBndWidth, int maxIter, int blurType) {
   const float blurThreshold = 0.98f;
   const int doCvExtrapol = trunc_f(vec_max_norm(c, vel, d) + 4);
-  if (doCvExtrapol > (1 << 16))
+  if (doCvExtrapol > (1 << 16)) {
+    check_device_errors(c);  // a kernel that gave up is the likelier cause
     fail(FLOF_E_NAN, "extrapolation sweep count out of range (non-finite or huge velocities)");
+  }
   if (!(postVelBlur < 1e30f) && postVelBlur == postVelBlur)
     fail(FLOF_E_ARG, "postVelBlur must be finite");
   DBuf marker(c, real_bytes(d)), tmp(c, vec_bytes(d));

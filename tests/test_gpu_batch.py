@@ -52,6 +52,32 @@ def test_batch_equals_single_calls(gpu):
     ctx.close()
 
 
+def test_fresh_workers_many_streams(gpu):
+    """Sixteen fresh worker contexts build their blur tables during the first
+    solves while the others already run.  The tables must be on the device
+    before the first blur reads them: every result equals the single call's."""
+    P = dict(FLOF, cgAccuracy=1e-4, multiStep=3, doFinalProject=True)
+    dims = (24, 24, 24, 16)
+    ps = []
+    for k in range(32):
+        s0, s1 = synth.random_pair_scenes(5000 + k)
+        ps.append((dims, synth.flow_input(s0, dims), synth.flow_input(s1, dims)))
+    ref_ctx = F.Context(0)
+    vs, a, b = grids(ref_ctx, ps)
+    single = []
+    for v, x, y in zip(vs, a, b):
+        F.opticalFlowMultiscale4d(v, x, y, **P)
+        single.append(v.to_numpy())
+    ref_ctx.close()
+    for rep in range(3):
+        ctx = F.Context(0)  # new context: new workers, empty table caches
+        vs, a, b = grids(ctx, ps)
+        F.opticalFlowMultiscale4d_batch(vs, a, b, workers=16, **P)
+        for q in range(len(ps)):
+            assert np.array_equal(vs[q].to_numpy(), single[q]), (rep, q)
+        ctx.close()
+
+
 def test_autotuned_solves_agree(gpu):
     ps = pairs()[:3]
     ctx = F.Context(0)
