@@ -211,8 +211,9 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *ctx, flof_grid *vel,
  * parameters and any grid sizes (vels[q], i0s[q], i1s[q] of one size per q).
  * They run concurrently on `workers` worker streams of the context, each
  * driven by its own host thread; workers <= 0 picks the count from the
- * sizes.  Every solve gives the same result as the single call on the same
- * grids.  errs (nullable) receives n error metrics. */
+ * smallest size.  At most 4M cells of solves are in flight at once, so a
+ * larger solve runs alone.  Every solve gives the same result as the single
+ * call on the same grids.  errs (nullable) receives n error metrics. */
 FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *ctx, int n,
                                                 flof_grid *const *vels,
                                                 const flof_grid *const *i0s,

@@ -6,9 +6,12 @@
 // a buffer pool and the PCG state, and one host thread drives it through the
 // same multiscale driver as the single call, so kernels of different solves
 // overlap on the GPU and one solve's host round trip hides behind another's
-// kernels.  Solves are handed out largest first from a shared counter.
+// kernels.  Solves are handed out largest first from a shared counter, and
+// a budget of cells in flight keeps large solves, which fill the GPU alone,
+// from running side by side.
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
 #include <mutex>
 #include <thread>
 
@@ -31,22 +34,46 @@ flof_ctx *worker(flof_ctx *c, size_t q) {
   return c->workers[q];
 }
 
-// Worker count when the caller leaves it open: enough streams that about
-// 64M cells of the largest solve are in flight (one 64^4 solve alone keeps
-// the PCG kernels near the HBM roofline), at most 16 and at most one per
-// solve.
+// Cells of the solves in flight at once.  A solve of a few million cells
+// keeps the PCG kernels near the HBM roofline on its own (on GB300: 3.5M-cell
+// solves gain nothing from a second stream, 1M-cell solves 1.4x from several,
+// 0.2M-cell solves 2.8x from sixteen), so a larger solve runs alone and
+// smaller ones share the budget.
+constexpr long long kCellsInFlight = 4ll << 20;
+
+// Worker count when the caller leaves it open: enough streams that the
+// smallest solves fill the budget, at most 16 and at most one per solve.
 int auto_workers(const std::vector<long long> &cells) {
-  long long total = 0, big = 0;
-  for (long long n : cells) {
-    total += n;
-    big = n > big ? n : big;
-  }
-  int w = (int)((64ll << 20) / (big > 0 ? big : 1));
+  long long small = cells.empty() ? 1 : cells[0];
+  for (long long n : cells) small = n < small ? n : small;
+  long long w = kCellsInFlight / (small > 0 ? small : 1);
   if (w < 1) w = 1;
   if (w > 16) w = 16;
-  if (w > (int)cells.size()) w = (int)cells.size();
-  return w;
+  if (w > (long long)cells.size()) w = (long long)cells.size();
+  return (int)w;
 }
+
+// Shares of the cells budget: a solve waits until its share fits; a solve
+// larger than the budget takes all of it.
+struct CellBudget {
+  std::mutex mu;
+  std::condition_variable cv;
+  long long used = 0;
+  long long acquire(long long n) {
+    if (n > kCellsInFlight) n = kCellsInFlight;
+    std::unique_lock<std::mutex> lk(mu);
+    cv.wait(lk, [&] { return used + n <= kCellsInFlight; });
+    used += n;
+    return n;
+  }
+  void release(long long n) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      used -= n;
+    }
+    cv.notify_all();
+  }
+};
 
 }  // namespace
 
@@ -93,6 +120,7 @@ FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *c, int n, flof_grid *c
     CK(cudaEventDestroy(ready));
 
     std::atomic<int> next(0);
+    CellBudget budget;
     std::mutex mu;
     int first_status = FLOF_OK;
     std::string first_msg;
@@ -103,8 +131,10 @@ FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *c, int n, flof_grid *c
         if (k >= n) break;
         const int q = order[k];
         float e = 0.f;
+        const long long share = budget.acquire(cells[q]);
         const int st = flof_opticalFlowMultiscale4d(w, vels[q], i0s[q], i1s[q], params, &e,
                                                     nullptr);
+        budget.release(share);
         if (st != FLOF_OK) {
           std::lock_guard<std::mutex> lk(mu);
           if (first_status == FLOF_OK) {
