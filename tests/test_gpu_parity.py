@@ -173,6 +173,25 @@ def test_opticalflow4d_single_level(gpu, orc, blur, ws):
     assert rel_l2(gv.to_numpy(), want) < REL_L2_DEFO
 
 
+# Solves cut off after a few iterations: the last x update is applied by the
+# direction kernel after the update has ended the solve (cgMaxIter reached).
+@pytest.mark.parametrize("max_iter", [0, 1, 2, 5])
+def test_opticalflow4d_iteration_cap(gpu, orc, max_iter):
+    dims = (20, 22, 18, 16)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    want, wit, _ = orc.opticalFlow4d(zv, i0, i1, 0.001, 0.0001, 0.0, 1e-8, -1.0, max_iter)
+    gv = grid_of(zv)
+    it, _ = F.opticalFlow4d(gv, grid_of(i0), grid_of(i1), wSmooth=0.001, wEnergy=0.0001,
+                            postVelBlur=0.0, cgAccuracy=1e-8, cgMaxIter=max_iter)
+    got = gv.to_numpy()
+    assert it == wit == max_iter
+    if max_iter == 0:
+        assert not np.any(got) and not np.any(want)
+    else:
+        assert rel_l2(got, want) < 1e-5
+
+
 # the second size leaves partial tiles in x, y and t in the staged kernels;
 # the large velocities send samples past the borders, where the weights clamp
 @pytest.mark.parametrize("dims,vscale", [((20, 20, 20, 16), 0.8), ((37, 21, 19, 15), 0.8),
