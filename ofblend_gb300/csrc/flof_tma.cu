@@ -114,11 +114,14 @@ __device__ __forceinline__ float4 unpack4(const P4 &v) {
   return r;
 }
 __device__ __forceinline__ float4 unpack4(const float4 &v) { return v; }
-__device__ __forceinline__ void mac4(float4 &v, float w, const float4 &a) {
-  v.x += w * a.x;
-  v.y += w * a.y;
-  v.z += w * a.z;
-  v.w += w * a.w;
+__device__ __forceinline__ float4 mul4(float w, const float4 &a) {
+  return make_float4(w * a.x, w * a.y, w * a.z, w * a.w);
+}
+__device__ __forceinline__ void add4(float4 &v, const float4 &p) {
+  v.x += p.x;
+  v.y += p.y;
+  v.z += p.z;
+  v.w += p.w;
 }
 
 template <int S>
@@ -288,19 +291,34 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
         for (int o = 0; o < DT; ++o) {
           const int vt = vt0 - o;
           if (vt < -S || vt > S) continue;
+          if constexpr (MODE == 0) {
+            // Output rows at y offsets +-ay use the same weights, so the
+            // rounded products w * a are formed once per |yj| and added to
+            // each of those rows in the usual xi order.
 #pragma unroll
-          for (int q = 0; q < RY; ++q) {
-            const int yj = k - q - S;
-            if (yj < -S || yj > S) continue;
-            if constexpr (MODE == 0) {
-              const int base = vt * vt + zk * zk + yj * yj;
-              float wx[S + 1];
+            for (int ay = 0; ay <= S; ++ay) {
+              bool used = false;
 #pragma unroll
-              for (int e = 0; e <= S; ++e) wx[e] = wsh[base + e * e];
+              for (int q = 0; q < RY; ++q) used |= (k - q - S == ay) || (k - q - S == -ay);
+              if (!used) continue;
+              const int base = vt * vt + zk * zk + ay * ay;
+              float4 prod[2 * S + 1];
 #pragma unroll
               for (int xi = -S; xi <= S; ++xi)
-                mac4(val[oz][o][q], wx[xi < 0 ? -xi : xi], a[xi + S]);
-            } else {
+                prod[xi + S] = mul4(wsh[base + xi * xi], a[xi + S]);
+#pragma unroll
+              for (int q = 0; q < RY; ++q) {
+                const int yj = k - q - S;
+                if (yj != ay && yj != -ay) continue;
+#pragma unroll
+                for (int xi = -S; xi <= S; ++xi) add4(val[oz][o][q], prod[xi + S]);
+              }
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < RY; ++q) {
+              const int yj = k - q - S;
+              if (yj < -S || yj > S) continue;
 #pragma unroll
               for (int xi = -S; xi <= S; ++xi) acc4(val[oz][o][q], a[xi + S]);
             }
