@@ -172,6 +172,20 @@ FLOF_API void *flof_grid_data(flof_grid *g);
 /* Host <-> device copies of the whole grid (bytes = cells * 4 * ncomp). */
 FLOF_API int flof_grid_upload(flof_grid *g, const void *host);
 FLOF_API int flof_grid_download(const flof_grid *g, void *host);
+/* Asynchronous copies on the context's copy stream, so that transfers
+ * overlap the kernels of the context stream (no counterpart in the
+ * reference).  Each copy starts after the work queued on the context stream
+ * when it is issued.  After an upload, call flof_grid_copy_wait before work
+ * that reads the grid; after a download, call it before work that writes the
+ * grid.  flof_grid_copy_wait makes the context stream wait on the device for
+ * the grid's last asynchronous copy; the host does not block.
+ * flof_ctx_copies_sync waits on the host for all of them, and so does
+ * flof_ctx_synchronize.  Host buffers must stay valid until then; pinned
+ * buffers give the overlap, pageable ones are staged synchronously. */
+FLOF_API int flof_grid_upload_async(flof_grid *g, const void *host);
+FLOF_API int flof_grid_download_async(flof_grid *g, void *host);
+FLOF_API int flof_grid_copy_wait(flof_grid *g);
+FLOF_API int flof_ctx_copies_sync(flof_ctx *ctx);
 
 /* Grid4d methods (grid4d.cpp:198-412).  Constants are float[4]; Real grids
  * use element 0. */

@@ -110,6 +110,10 @@ SIGNATURES = {
     "flof_grid_data": (P, [P]),
     "flof_grid_upload": (I, [P, P]),
     "flof_grid_download": (I, [P, P]),
+    "flof_grid_upload_async": (I, [P, P]),
+    "flof_grid_download_async": (I, [P, P]),
+    "flof_grid_copy_wait": (I, [P]),
+    "flof_ctx_copies_sync": (I, [P]),
     "flof_grid_copyFrom": (I, [P, P]),
     "flof_grid_add": (I, [P, P]),
     "flof_grid_sub": (I, [P, P]),

@@ -89,6 +89,10 @@ class Context:
     def synchronize(self):
         check(self.lib.flof_ctx_synchronize(self.h))
 
+    def copies_sync(self):
+        """Wait on the host for every asynchronous grid copy of the context."""
+        check(self.lib.flof_ctx_copies_sync(self.h))
+
     def kernel_launches(self) -> int:
         return int(self.lib.flof_ctx_kernel_launches(self.h))
 
@@ -204,6 +208,33 @@ class _Grid:
             out = np.empty(self.shape, dtype=np.float32)
         check(self.ctx.lib.flof_grid_download(self.h, out.ctypes.data_as(ctypes.c_void_p)))
         return out
+
+    # -- asynchronous host transfers (copy stream of the context) ---------------
+    def _host_buf(self, a):
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous
+                and a.size == int(np.prod(self.shape))):
+            raise FlofError(1, f"need a C-contiguous float32 array of {int(np.prod(self.shape))} "
+                               "floats (pinned for overlap)")
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    def upload_async(self, a):
+        """Queue host -> grid on the copy stream; call copy_wait() before
+        work that reads the grid.  `a` must stay alive until the copy ends."""
+        check(self.ctx.lib.flof_grid_upload_async(self.h, self._host_buf(a)))
+        return self
+
+    def download_async(self, out):
+        """Queue grid -> host on the copy stream after the work queued so far;
+        call copy_wait() before work that writes the grid, and
+        Context.copies_sync() before reading `out`."""
+        check(self.ctx.lib.flof_grid_download_async(self.h, self._host_buf(out)))
+        return out
+
+    def copy_wait(self):
+        """The context stream waits (on the device) for this grid's last
+        asynchronous copy."""
+        check(self.ctx.lib.flof_grid_copy_wait(self.h))
+        return self
 
     # -- Grid4d methods (grid4d.h:205-236) --------------------------------------
     def copyFrom(self, a, copyType=True):

@@ -770,6 +770,7 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   if (!c) return FLOF_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   for (auto &kv : c->lats) {
     if (kv.second.vt) c->pool.put(kv.second.vt);
     if (kv.second.defo) grid_unpin(const_cast<flof_grid *>(kv.second.defo));
@@ -800,6 +801,8 @@ FLOF_API int flof_ctx_destroy(flof_ctx *c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (auto &kv : c->wsum_cache) cudaFree(kv.second);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->copy_order) cudaEventDestroy(c->copy_order);
   for (flof_ctx *w : c->workers) flof_ctx_destroy(w);
   delete c;
   // teardown reports nothing; leave no error behind for the next call
@@ -811,6 +814,7 @@ FLOF_API int flof_ctx_synchronize(flof_ctx *c) {
   return guarded([&] {
     need(c != nullptr, "ctx is NULL");
     CK(cudaStreamSynchronize(c->stream));
+    if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
   });
 }
 
@@ -968,11 +972,35 @@ FLOF_API int flof_grid_dims(const flof_grid *g, int dims[4], int *elem) {
 
 FLOF_API void *flof_grid_data(flof_grid *g) { return g ? g->d : nullptr; }
 
+namespace {
+// The context stream waits (on the device) for the grid's last asynchronous
+// transfer.
+void after_grid_copy(const flof_grid *g) {
+  if (g->copy_ev) CK(cudaStreamWaitEvent(g->ctx->stream, g->copy_ev, 0));
+}
+
+// Queues a host transfer of the whole grid on the context's copy stream,
+// after everything already queued on the context stream.
+void grid_copy_async(flof_grid *g, void *dst, const void *src, cudaMemcpyKind kind) {
+  flof_ctx *c = g->ctx;
+  if (!c->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->copy_order, cudaEventDisableTiming));
+  }
+  if (!g->copy_ev) CK(cudaEventCreateWithFlags(&g->copy_ev, cudaEventDisableTiming));
+  CK(cudaEventRecord(c->copy_order, c->stream));
+  CK(cudaStreamWaitEvent(c->copy_stream, c->copy_order, 0));
+  CK(cudaMemcpyAsync(dst, src, g->bytes(), kind, c->copy_stream));
+  CK(cudaEventRecord(g->copy_ev, c->copy_stream));
+}
+}  // namespace
+
 FLOF_API int flof_grid_upload(flof_grid *g, const void *host) {
   return guarded([&] {
     need_grid(g, "grid");
     need(host != nullptr, "host buffer is NULL");
     set_ctx_device(g->ctx);
+    after_grid_copy(g);
     CK(cudaMemcpyAsync(g->d, host, g->bytes(), cudaMemcpyHostToDevice, g->ctx->stream));
     CK(cudaStreamSynchronize(g->ctx->stream));
   });
@@ -983,8 +1011,43 @@ FLOF_API int flof_grid_download(const flof_grid *g, void *host) {
     need_grid(g, "grid");
     need(host != nullptr, "host buffer is NULL");
     set_ctx_device(g->ctx);
+    after_grid_copy(g);
     CK(cudaMemcpyAsync(host, g->d, g->bytes(), cudaMemcpyDeviceToHost, g->ctx->stream));
     CK(cudaStreamSynchronize(g->ctx->stream));
+  });
+}
+
+FLOF_API int flof_grid_upload_async(flof_grid *g, const void *host) {
+  return guarded([&] {
+    need_grid(g, "grid");
+    need(host != nullptr, "host buffer is NULL");
+    set_ctx_device(g->ctx);
+    grid_copy_async(g, g->d, host, cudaMemcpyHostToDevice);
+  });
+}
+
+FLOF_API int flof_grid_download_async(flof_grid *g, void *host) {
+  return guarded([&] {
+    need_grid(g, "grid");
+    need(host != nullptr, "host buffer is NULL");
+    set_ctx_device(g->ctx);
+    grid_copy_async(g, host, g->d, cudaMemcpyDeviceToHost);
+  });
+}
+
+FLOF_API int flof_grid_copy_wait(flof_grid *g) {
+  return guarded([&] {
+    need_grid(g, "grid");
+    set_ctx_device(g->ctx);
+    after_grid_copy(g);
+  });
+}
+
+FLOF_API int flof_ctx_copies_sync(flof_ctx *c) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    set_ctx_device(c);
+    if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream));
   });
 }
 

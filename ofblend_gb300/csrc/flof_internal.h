@@ -124,6 +124,10 @@ struct flof_ctx {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // asynchronous host transfers (flof_grid_*_async): their own stream, ordered
+  // after the work queued on `stream` when each copy is issued
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_order = nullptr;
   fh::Pool pool;
   CGState *st = nullptr;    // device
   CGState *st_h = nullptr;  // pinned host mirror
@@ -175,6 +179,8 @@ struct flof_grid {
   // grid is deferred until the last Finish releases it.
   int pins = 0;
   bool destroy_pending = false;
+  // completion of the grid's last asynchronous host transfer (null: none yet)
+  cudaEvent_t copy_ev = nullptr;
   Dims4 D() const { return Dims4{dims[0], dims[1], dims[2], dims[3]}; }
   int nc() const { return elem == FLOF_VEC4 ? 4 : 1; }
   long long cells() const { return (long long)dims[0] * dims[1] * dims[2] * dims[3]; }
@@ -188,6 +194,7 @@ namespace fh {
 // Frees a grid's storage (owned grids) and its handle.  A grid whose context
 // is gone has no storage left (the context freed it) and only the handle goes.
 inline void grid_free(flof_grid *g) {
+  if (g->copy_ev) cudaEventSynchronize(g->copy_ev);  // no transfer outlives the storage
   if (g->ctx) {
     if (g->owned && g->d) {
       cudaSetDevice(g->ctx->device);
@@ -196,6 +203,7 @@ inline void grid_free(flof_grid *g) {
     }
     g->ctx->grids.erase(g);
   }
+  if (g->copy_ev) cudaEventDestroy(g->copy_ev);
   delete g;
 }
 
