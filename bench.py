@@ -323,12 +323,50 @@ CPU_SAMPLE = ("one full opticalFlowMultiscale4d 0->1 at 32^4 (flof parameters, s
               "time ratio of 15.9 measured at cgAccuracy 0.01")
 
 
+# ---------------------------------------------------------------------------
+# ranks: one process per GPU, replicas of the whole workload (no data-path
+# collective); these helpers run on any torch.distributed backend
+# ---------------------------------------------------------------------------
+def init_ranks(world, local, backend="nccl"):
+    """Join the process group of a multi-rank run (NCCL on the GPU machine; the
+    tests use gloo on CPU)."""
+    if world <= 1:
+        return
+    import torch
+    import torch.distributed as td
+    if backend == "nccl":
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        td.init_process_group(backend)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(x, world, device="cuda"):
+    """The slowest rank's time: the whole job ends when it does."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, seconds):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time."""
+    return units_per_rank * world / seconds
+
+
 def run_gpu(a):
     import torch
     rank, world, local = dist()
-    if world > 1:
-        import torch.distributed as td
-        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    init_ranks(world, local)
     torch.cuda.set_device(local)
     import ofblend_gb300 as F
     from ofblend_gb300 import synth
@@ -340,8 +378,7 @@ def run_gpu(a):
     for _ in range(max(a.warmup, 0)):
         W.step()
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     uuid = None
     try:
         uuid = str(torch.cuda.get_device_properties(local).uuid)
@@ -359,8 +396,7 @@ def run_gpu(a):
         W.step()
     e1.record(stream)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
+    barrier(world)
     launches = ctx.kernel_launches() - l0
     ms = e0.elapsed_time(e1)
     # A second pass of the same steps with a CUDA event pair around every
@@ -377,14 +413,10 @@ def run_gpu(a):
     clk = clocks.stop()
     recs = ctx.profile_records()
     ctx.profile(False)
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    solves = 2 * a.steps * world
+    ms_max = max_over_ranks(ms, world)
     if a.steps <= 0:
         raise SystemExit("--steps must be positive")
-    value = solves / (ms_max * 1e-3)
+    value = job_rate(2 * a.steps, world, ms_max * 1e-3)
     peak, peak_kind = measured_peaks()
     rl, share = roofline(recs, a.res, peak, peak_kind, ncu_traffic())
     rl["region"] = "profiled pass of the same steps, one CUDA event pair per launch"
@@ -404,17 +436,13 @@ def run_gpu(a):
     if a.e2e_steps > 0:
         W.step_e2e(pinned, sink, ctx)
         torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+        barrier(world)
         t0 = time.perf_counter()
         for _ in range(a.e2e_steps):
             W.step_e2e(pinned, sink, ctx)
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        te = torch.tensor([e2e_s], device="cuda")
-        if world > 1:
-            torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-        e2e_val = round(2 * a.e2e_steps * world / float(te.item()), 4)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+        e2e_val = round(job_rate(2 * a.e2e_steps, world, e2e_s), 4)
 
     st = W.stats
     iters = [s["solves"] for s in st]
