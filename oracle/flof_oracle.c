@@ -4,7 +4,8 @@
  * TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle for the
  * GB300 library in ofblend_gb300/.  Only tests/, __graft_entry__.smoke() and
  * the cpu_baseline / reference legs of bench.py may load it, and only as the
- * checker or as the timed CPU baseline.  The product never calls it.
+ * oracle the GPU results are compared with or as the timed CPU baseline.  The
+ * product never calls it.
  *
  * What it is: a from-scratch C restatement of the reference's algorithm,
  * following the reference's operation order so that per-cell results can be

@@ -1,6 +1,6 @@
 """CPU oracle of the learned warm start network (numpy, float64).
 
-TEST INFRASTRUCTURE ONLY: the checker of ofblend_gb300's network kernels
+TEST INFRASTRUCTURE ONLY: the oracle of ofblend_gb300's network kernels
 (csrc/flof_net.cu, csrc/flof_model.cu).  The network has no counterpart in
 the reference, so this is a from-scratch restatement of the same
 architecture, used for the forward pass and, by finite differences, for the
