@@ -328,7 +328,7 @@ CPU_SAMPLE = ("one full opticalFlowMultiscale4d 0->1 at 32^4 (flof parameters, s
 # collective); these helpers run on any torch.distributed backend
 # ---------------------------------------------------------------------------
 def init_ranks(world, local, backend="nccl"):
-    """Join the process group of a multi-rank run (NCCL on the GPU machine; the
+    """Join the process group of a multi-rank run (NCCL between GPUs; the
     tests use gloo on CPU)."""
     if world <= 1:
         return
