@@ -226,8 +226,10 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *ctx, flof_grid *vel,
  * They run concurrently on `workers` worker streams of the context, each
  * driven by its own host thread; workers <= 0 picks the count from the
  * smallest size.  At most 4M cells of solves are in flight at once, so a
- * larger solve runs alone.  Every solve gives the same result as the single
- * call on the same grids.  errs (nullable) receives n error metrics. */
+ * larger solve runs alone.  With params->warmStart and a model attached to
+ * ctx, the solves run one after another on ctx itself (the model's buffers
+ * serve one prediction at a time).  Every solve gives the same result as the
+ * single call on the same grids.  errs (nullable) receives n error metrics. */
 FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *ctx, int n,
                                                 flof_grid *const *vels,
                                                 const flof_grid *const *i0s,

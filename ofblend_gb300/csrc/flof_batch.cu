@@ -101,6 +101,19 @@ FLOF_API int flof_opticalFlowMultiscale4d_batch(flof_ctx *c, int n, flof_grid *c
       cells[q] = vels[q]->cells();
     }
     set_ctx_device(c);
+    if (params && params->warmStart && c->model) {
+      // The attached model keeps its activations in one set of buffers on
+      // its context's stream, so warm-started solves run in turn on this
+      // context: the single call's results, one after another.
+      for (int q = 0; q < n; ++q) {
+        float e = 0.f;
+        const int st = flof_opticalFlowMultiscale4d(c, vels[q], i0s[q], i1s[q], params, &e,
+                                                    nullptr);
+        if (st != FLOF_OK) fail(st, "solve " + std::to_string(q) + ": " + g_last_error);
+        if (errs) errs[q] = e;
+      }
+      return;
+    }
     int nw = workers > 0 ? workers : auto_workers(cells);
     if (nw > n) nw = n;
     // largest first

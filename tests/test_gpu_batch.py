@@ -78,6 +78,33 @@ def test_fresh_workers_many_streams(gpu):
         ctx.close()
 
 
+def test_batch_with_warm_start_equals_single_calls(gpu):
+    """With a model attached, warm-started batch solves give the single
+    calls' results (they run in turn on the calling context)."""
+    ctx = F.Context(0)
+    m = F.Model(16, ctx=ctx, seed=11)
+    m.attach()
+    dims = (32, 32, 32, 32)  # coarsest level 16^4: the model's grid
+    ps = []
+    for k in range(3):
+        s0, s1 = synth.random_pair_scenes(7000 + k)
+        ps.append((dims, synth.flow_input(s0, dims), synth.flow_input(s1, dims)))
+    vs, a, b = grids(ctx, ps)
+    single = []
+    flags = []
+    for v, x, y in zip(vs, a, b):
+        F.opticalFlowMultiscale4d(v, x, y, warmStart=True, **FLOF)
+        single.append(v.to_numpy())
+        flags.append(F.last_solve_stats()["warm_start"])
+        v.setConst(0.0)
+    assert all(f in (0, 1) for f in flags)  # the prediction was tried
+    F.opticalFlowMultiscale4d_batch(vs, a, b, workers=4, warmStart=True, **FLOF)
+    for q in range(len(ps)):
+        assert np.array_equal(vs[q].to_numpy(), single[q]), q
+    m.detach()
+    ctx.close()
+
+
 def test_autotuned_solves_agree(gpu):
     ps = pairs()[:3]
     ctx = F.Context(0)
