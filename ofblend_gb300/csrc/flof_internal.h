@@ -313,8 +313,9 @@ inline void check_device_errors(flof_ctx *c) {
   if (e) {
     CK(cudaMemsetAsync(c->dev_err, 0, sizeof(int), c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    fail(FLOF_E_TIMEOUT, "a bounded wait on a TMA copy gave up (device error " +
-                             std::to_string(e) + ")");
+    fail(FLOF_E_TIMEOUT, std::string("a bounded wait on ") +
+                             (e == flof::FLOF_DEV_ERR_TC_TIMEOUT ? "tensor-core MMAs" : "a TMA copy") +
+                             " gave up (device error " + std::to_string(e) + ")");
   }
 }
 

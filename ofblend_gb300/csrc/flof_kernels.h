@@ -208,6 +208,8 @@ void launch_expol_slab(const float4 *in, float4 *out, const float *mark, Dims4 d
 // uses the cp.async kernels).  A block whose bounded mbarrier wait runs out
 // stores FLOF_DEV_ERR_TMA_TIMEOUT in *err and returns.
 constexpr int FLOF_DEV_ERR_TMA_TIMEOUT = 1;
+// a tensor-core convolution block whose bounded wait on its MMAs ran out
+constexpr int FLOF_DEV_ERR_TC_TIMEOUT = 2;
 bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const float *wtab,
                       const float *wsum_dev, int zero_border, int *err, cudaStream_t st);
 // The TMA extrapolation sweep writes only the cells it updates (unmarked
@@ -289,5 +291,27 @@ void net_round_bf16(const float *w, float *wq, long long n, cudaStream_t s);
 void net_input(const float *i0, const float *i1, float *x, long long V, float scale,
                cudaStream_t s);
 void net_add_into(float *a, const float *b, long long n, cudaStream_t s);
+
+// Tensor-core (tcgen05) versions of the 3^4 convolutions (flof_conv_tc.cu).
+// The *_ok predicates name the shapes they take; the weights enter as BF16
+// copies made by net_weights_tc: WB[tap][ci][co] (input gradient) and
+// WT[co][kpad] (forward, rows of net_tc_kpad entries, zero tail).  `work`
+// holds net_tc_work(...) floats; a block whose bounded wait runs out stores
+// FLOF_DEV_ERR_TC_TIMEOUT in *err.
+bool net_tc_fwd_ok(int cin, int cout, int ks);
+bool net_tc_bwd_data_ok(int cin, int cout, int ks);
+bool net_tc_bwd_weight_ok(int cin, int cout, int ks);
+int net_tc_kpad(int cin, int ks);
+size_t net_tc_work(int rin, int rout, int cin, int cout, int ks);
+void net_weights_tc(const float *wq, uint16_t *wb, uint16_t *wt, int cin, int cout, int ks,
+                    cudaStream_t s);
+void net_tc_conv_fwd(const float *in, const uint16_t *wt, const float *b, float *out,
+                     float *work, int rin, int rout, int cin, int cout, int stride, int relu,
+                     int *err, cudaStream_t s);
+void net_tc_conv_bwd_data(const float *dout, const uint16_t *wb, float *din, float *work,
+                          int rin, int rout, int cin, int cout, int stride, int *err,
+                          cudaStream_t s);
+void net_tc_conv_bwd_weight(const float *in, const float *dout, float *dw, float *work, int rin,
+                            int rout, int cin, int cout, int stride, int *err, cudaStream_t s);
 
 }  // namespace flof

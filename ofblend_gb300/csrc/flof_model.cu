@@ -15,6 +15,7 @@
 //   O conv1 16->4 (the velocity, in coarse cells)
 // Inputs are the coarse i0, i1 times INPUT_SCALE (the solver's lsFactor
 // undone: SDF values in cells).
+#include <algorithm>
 #include <random>
 
 #include "flof_internal.h"
@@ -44,7 +45,11 @@ struct flof_model {
   long long woff[8], boff[8], wsize[8];
   float *w = nullptr, *wq = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
   float *scratch = nullptr;  // one layer's weight gradient
-  float *work = nullptr;     // split-reduction slices of a weight gradient
+  float *work = nullptr;     // split-reduction slices of a convolution
+  // BF16 weight copies of the tensor-core convolutions: WB (the weights'
+  // own order) at woff, WT (transposed, rows of kpad) at wtoff
+  uint16_t *wb = nullptr, *wt = nullptr;
+  long long wtoff[8];
   int step = 0;
   // activations and their gradients
   float *x = nullptr, *a[7] = {}, *c5 = nullptr, *c6 = nullptr, *out = nullptr;
@@ -70,6 +75,16 @@ struct flof_model {
 namespace {
 
 cudaStream_t S(flof_model *m) { return m->ctx->stream; }
+int *E(flof_model *m) { return m->ctx->dev_err; }
+
+// the BF16 weight copies follow every change of the working weights
+void refresh_tc_weights(flof_model *m) {
+  for (int l = 0; l < 8; ++l) {
+    const LayerDef &L = LAYERS[l];
+    net_weights_tc(m->wq + m->woff[l], m->wb + m->woff[l], m->wt + m->wtoff[l], L.cin, L.cout,
+                   L.ks, S(m));
+  }
+}
 
 void forward(flof_model *m, const float *i0, const float *i1, float *out) {
   const int R = m->R;
@@ -77,8 +92,12 @@ void forward(flof_model *m, const float *i0, const float *i1, float *out) {
   net_input(i0, i1, m->x, m->V(1), INPUT_SCALE, s);
   auto conv = [&](int l, const float *in, float *o) {
     const LayerDef &L = LAYERS[l];
-    net_conv_fwd(in, m->wq + m->woff[l], m->wq + m->boff[l], o, R / L.rin_div, R / L.rout_div,
-                 L.cin, L.cout, L.ks, L.stride, L.relu, s);
+    if (net_tc_fwd_ok(L.cin, L.cout, L.ks))
+      net_tc_conv_fwd(in, m->wt + m->wtoff[l], m->wq + m->boff[l], o, m->work, R / L.rin_div,
+                      R / L.rout_div, L.cin, L.cout, L.stride, L.relu, E(m), s);
+    else
+      net_conv_fwd(in, m->wq + m->woff[l], m->wq + m->boff[l], o, R / L.rin_div,
+                   R / L.rout_div, L.cin, L.cout, L.ks, L.stride, L.relu, s);
   };
   conv(0, m->x, m->a[0]);
   conv(1, m->a[0], m->a[1]);
@@ -99,11 +118,21 @@ void layer_bwd(flof_model *m, int l, const float *in, const float *dy, float *di
   const int R = m->R;
   cudaStream_t s = S(m);
   const int rin = R / L.rin_div, rout = R / L.rout_div;
-  net_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.ks, L.stride, s);
+  if (net_tc_bwd_weight_ok(L.cin, L.cout, L.ks))
+    net_tc_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.stride,
+                           E(m), s);
+  else
+    net_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.ks, L.stride,
+                        s);
   net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l], s);
   net_bias_grad(dy, m->scratch, (long long)rout * rout * rout * rout, L.cout, s);
   net_add_into(m->grad + m->boff[l], m->scratch, L.cout, s);
-  if (din) net_conv_bwd_data(dy, m->wq + m->woff[l], din, rin, rout, L.cin, L.cout, L.ks, L.stride, s);
+  if (!din) return;
+  if (net_tc_bwd_data_ok(L.cin, L.cout, L.ks))
+    net_tc_conv_bwd_data(dy, m->wb + m->woff[l], din, m->work, rin, rout, L.cin, L.cout,
+                         L.stride, E(m), s);
+  else
+    net_conv_bwd_data(dy, m->wq + m->woff[l], din, rin, rout, L.cin, L.cout, L.ks, L.stride, s);
 }
 
 // loss of one sample, gradients added to m->grad
@@ -189,12 +218,19 @@ FLOF_API int flof_model_create(flof_ctx *c, int res, flof_model **out) {
     m->v = m->alloc(off);
     m->scratch = m->alloc(maxw);
     size_t maxwork = 0;
+    long long wtsize = 0;
     for (int l = 0; l < 8; ++l) {
       const LayerDef &L = LAYERS[l];
       const size_t wk = net_conv_bwd_weight_work(res / L.rout_div, L.cin, L.cout, L.ks);
-      maxwork = wk > maxwork ? wk : maxwork;
+      const size_t wt = net_tc_work(res / L.rin_div, res / L.rout_div, L.cin, L.cout, L.ks);
+      maxwork = std::max(maxwork, std::max(wk, wt));
+      m->wtoff[l] = wtsize;
+      wtsize += (long long)L.cout * net_tc_kpad(L.cin, L.ks);
     }
     m->work = m->alloc(maxwork);
+    m->wb = (uint16_t *)m->alloc((off + 1) / 2);
+    m->wt = (uint16_t *)m->alloc((wtsize + 1) / 2);
+    CK(cudaMemsetAsync(m->wt, 0, wtsize * sizeof(uint16_t), c->stream));
     const long long V1 = m->V(1), V2 = m->V(2), V4 = m->V(4);
     m->x = m->alloc(V1 * 2);
     const long long asz[7] = {V1 * 16, V2 * 32, V2 * 32, V4 * 64, V4 * 64, V2 * 32, V1 * 16};
@@ -268,6 +304,7 @@ FLOF_API int flof_model_init(flof_model *m, unsigned long long seed) {
     CK(cudaMemcpyAsync(m->w, h.data(), m->nparams * sizeof(float), cudaMemcpyHostToDevice,
                        S(m)));
     net_round_bf16(m->w, m->wq, m->nparams, S(m));
+    refresh_tc_weights(m);
     CK(cudaMemsetAsync(m->m, 0, m->nparams * sizeof(float), S(m)));
     CK(cudaMemsetAsync(m->v, 0, m->nparams * sizeof(float), S(m)));
     m->step = 0;
@@ -293,6 +330,7 @@ FLOF_API int flof_model_set_params(flof_model *m, const float *host) {
     set_ctx_device(m->ctx);
     CK(cudaMemcpyAsync(m->w, host, m->nparams * sizeof(float), cudaMemcpyHostToDevice, S(m)));
     net_round_bf16(m->w, m->wq, m->nparams, S(m));
+    refresh_tc_weights(m);
     CK(cudaStreamSynchronize(S(m)));
   });
 }
@@ -308,6 +346,7 @@ FLOF_API int flof_model_predict(flof_model *m, const flof_grid *i0, const flof_g
     set_ctx_device(m->ctx);
     forward(m, i0->f(), i1->f(), vel->f());
     CK(cudaStreamSynchronize(S(m)));
+    check_device_errors(m->ctx);
   });
 }
 
@@ -331,6 +370,7 @@ FLOF_API int flof_model_loss_grad(flof_model *m, const flof_grid *i0, const flof
       CK(cudaMemcpyAsync(grad_host, m->grad, m->nparams * sizeof(float), cudaMemcpyDeviceToHost,
                          S(m)));
     CK(cudaStreamSynchronize(S(m)));
+    check_device_errors(m->ctx);
     if (loss) *loss = *m->hloss;
   });
 }
@@ -358,8 +398,10 @@ FLOF_API int flof_model_train_step(flof_model *m, int n, const flof_grid *const 
     }
     m->step++;
     net_adam(m->w, m->wq, m->grad, m->m, m->v, m->nparams, lr, m->step, 1.f / n, S(m));
+    refresh_tc_weights(m);
     CK(cudaMemcpyAsync(m->hloss, m->dloss, sizeof(double), cudaMemcpyDeviceToHost, S(m)));
     CK(cudaStreamSynchronize(S(m)));
+    check_device_errors(m->ctx);
     if (loss) *loss = *m->hloss / n;
   });
 }
