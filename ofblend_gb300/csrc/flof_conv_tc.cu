@@ -10,12 +10,16 @@
 //   weight gradient:          acc += A_hi B_hi + A_lo B_hi + A_hi B_lo (3 MMAs)
 // with FP32 accumulation in tensor memory.
 //
-// Per block: 128 threads gather a 128 x 64 reduction chunk of the operand
+// Per block: 256 threads gather a 128 x 64 reduction chunk of the operand
 // (im2col on the fly: voxel rows x (tap, channel), or (tap, channel) rows x
 // voxels for the weight gradient) through registers into shared memory in
-// the no-swizzle K-major layout (flof_tcgen05.cuh), while thread 0's MMAs of
-// the previous chunk run; two stages, each released by a tcgen05.commit on
-// its mbarrier.  Layers with few row tiles split the reduction into slices
+// the 128-byte-swizzled K-major layout (flof_tcgen05.cuh), while thread 0's
+// MMAs of the previous chunk run; two stages, each released by a
+// tcgen05.commit on its mbarrier.  The forward and input-gradient gathers
+// run along channels (16 lanes read 256 contiguous bytes of a row), the
+// weight-gradient gather along the (tap, channel) rows.  The weight
+// gradient carries one more row of ones, whose products are the bias
+// gradient.  Layers with few row tiles split the reduction into slices
 // written to a work buffer and summed in slice order (deterministic), with
 // the bias and ReLU applied there.
 //
@@ -37,7 +41,8 @@ using namespace tc;
 
 constexpr int TB_M = 128;  // rows per block (the MMA's M)
 constexpr int TB_K = 64;   // reduction entries per chunk (four K = 16 MMAs)
-constexpr int TB_T = 128;  // threads
+constexpr int TB_T = 256;  // threads: two per row, each staging half the reduction groups
+constexpr int KG_T = 8 * TB_M / TB_T;  // reduction groups (of 8) per thread and chunk
 constexpr int A_TILE = TB_M * TB_K * 2;  // bytes of one BF16 A tile
 
 struct TcArgs {
@@ -50,6 +55,7 @@ struct TcArgs {
   int rin, rout, cin, cout, stride;
   int M, N, K, Kpad;      // rows, columns, reduction length, WT row length
   int relu, kslice, ncols;
+  int bias_row;           // MODE 2: the last row is all ones (the bias gradient)
 };
 
 // (tap, channel) reduction entries of a 3^4 tap with offsets o in 0..2 per
@@ -59,6 +65,8 @@ struct TcArgs {
 struct TapEnt {
   int need, off;
 };
+
+__device__ const float kOne = 1.f;  // the weight gradient's bias row
 
 __device__ __forceinline__ void tap_digits(int tap, int o[4]) {
   o[0] = tap % 3;
@@ -79,14 +87,37 @@ __device__ __forceinline__ int edge_mask(const int s[4], int ext) {
   return m;
 }
 
+// weight gradient: voxel table of reduction chunk c (its 64 output voxels):
+// (input voxel of v * stride times cin, edge mask), bit 8 set past the
+// slice's end
+__device__ __forceinline__ void fill_vtab(int2 *vt, int tid, int kbeg, int c, int nch, int kend,
+                                          int rout, int rin, int stride, int cin) {
+  if (tid >= TB_K) return;
+  const int v = kbeg + c * TB_K + tid;
+  int2 e = make_int2(0, 0x100);
+  if (c < nch && v < kend) {
+    int s[4], q = v;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      s[a] = (q % rout) * stride;
+      q /= rout;
+    }
+    e = make_int2((s[0] + rin * (s[1] + rin * (s[2] + rin * s[3]))) * cin, edge_mask(s, rin));
+  }
+  vt[tid] = e;
+}
+
 template <int MODE, int VEC>
-__global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
-  extern __shared__ __align__(1024) unsigned char smem[];
+__global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
+  extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t bars[2];
   __shared__ uint32_t tbase;
-  __shared__ TapEnt taps[81];          // MODE 0
-  __shared__ int2 vtab[2][TB_K];       // MODE 2: (input voxel of v * stride, edge mask)
+  __shared__ TapEnt taps[81];     // MODE 0, and MODE 1 at stride 1
+  __shared__ int2 rows_s[TB_M];   // MODE 0/1: row table (see below)
+  __shared__ int2 vtab[2][TB_K];  // MODE 2: voxel tables of two chunks
 
+  // tiles start on 1024-byte boundaries (128-byte swizzle)
+  unsigned char *smem = smem_raw + ((1024u - (smem_addr(smem_raw) & 1023u)) & 1023u);
   const int tid = threadIdx.x, warp = tid >> 5;
   const int m0 = blockIdx.x * TB_M;
   const int N = p.N;
@@ -97,88 +128,93 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
   const int kpad_end = MODE == 0 ? min(p.Kpad, kbeg + p.kslice) : kend;
   const int nch = (kpad_end - kbeg + TB_K - 1) / TB_K;
   const int rin = p.rin, rout = p.rout;
-  const int is1 = rin, is2 = rin * rin, is3 = rin * rin * rin;  // input strides
+  // MODE 1 at stride 1 reads the output gradient like a forward pass with
+  // mirrored taps; at stride 2 it decodes each row's coordinates
+  const bool mirror = MODE == 1 && p.stride == 1;
 
   if (warp == 0) tmem_alloc(&tbase, (uint32_t)p.ncols);
   if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
   }
-  if (MODE == 0 && tid < 81) {
+  if ((MODE == 0 || mirror) && tid < 81) {
+    // grid the taps read: the input (MODE 0) or the output gradient (MODE 1)
+    const int e = MODE == 0 ? rin : rout;
     int o[4];
     tap_digits(tid, o);
-    int need = 0x100, off = 0;
-    const int st[4] = {1, is1, is2, is3};
+    int need = 0x100, off = 0, st = 1;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      need |= (o[a] == 0) << a;
-      need |= (o[a] == 2) << (4 + a);
-      off += (o[a] - 1) * st[a];
+      const int lo = MODE == 0 ? 0 : 2;  // the offset that falls off at coordinate 0
+      need |= (o[a] == lo) << a;
+      need |= (o[a] == 2 - lo) << (4 + a);
+      off += (MODE == 0 ? o[a] - 1 : 1 - o[a]) * st;
+      st *= e;
     }
     taps[tid] = TapEnt{need, off};
   }
-
-  // this thread's row
-  const int row = m0 + tid;
-  const bool rowvalid = row < p.M;
-  int rc[4] = {0, 0, 0, 0};     // MODE 0/1: voxel coordinates of the row
-  int rowlin = 0, rowmask = 0x100;  // MODE 0
-  int need_t = 0x100, tapoff_t = 0, ci_t = 0;  // MODE 2
-  if (MODE == 0 || MODE == 1) {
-    if (rowvalid) {
-      int v = row;
+  // row table: MODE 0: (input voxel of row * stride, edge mask);
+  // MODE 1 mirrored: (row's voxel, edge mask in the output-gradient grid);
+  // MODE 1 at stride 2: (packed coordinates, valid)
+  if ((MODE == 0 || MODE == 1) && tid < TB_M) {
+    const int row = m0 + tid;
+    int2 e = make_int2(0, MODE == 1 && !mirror ? 0 : 0x100);
+    if (row < p.M) {
       const int ext = MODE == 0 ? rout : rin;
+      int c[4], v = row;
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        rc[a] = v % ext;
+        c[a] = v % ext;
         v /= ext;
       }
-    }
-    if (MODE == 0 && rowvalid) {
-      int s[4];
+      if (MODE == 0) {
+        int s[4];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) s[a] = rc[a] * p.stride;
-      rowlin = s[0] + s[1] * is1 + s[2] * is2 + s[3] * is3;
-      rowmask = edge_mask(s, rin);
+        for (int a = 0; a < 4; ++a) s[a] = c[a] * p.stride;
+        e = make_int2(s[0] + rin * (s[1] + rin * (s[2] + rin * s[3])), edge_mask(s, rin));
+      } else if (mirror) {
+        e = make_int2(row, edge_mask(c, rout));
+      } else {
+        e = make_int2(c[0] | (c[1] << 8) | (c[2] << 16) | (c[3] << 24), 1);
+      }
     }
-  } else if (rowvalid) {
-    const int tap = row / p.cin;
-    ci_t = row - tap * p.cin;
+    rows_s[tid] = e;
+  }
+  // MODE 2: this thread's row (tap, ci) reads src_t[(e.x + off_t) & xmask_t]
+  // for each voxel e of the table that its `need` mask admits.  The bias
+  // row, and rows past the end (never stored), read the constant 1.
+  const int lrow = tid & (TB_M - 1), kgbase = (tid / TB_M) * KG_T;
+  const int row2 = m0 + lrow;
+  const float *src_t = &kOne;
+  int need_t = 0x100, off_t = 0, xmask_t = 0;
+  if (MODE == 2 && row2 < p.M - p.bias_row) {
+    const int tap = row2 / p.cin;
     int o[4];
     tap_digits(tap, o);
-    need_t = 0x100;
-    const int st[4] = {1, is1, is2, is3};
+    int st = 1, tapoff = 0;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       need_t |= (o[a] == 0) << a;
       need_t |= (o[a] == 2) << (4 + a);
-      tapoff_t += (o[a] - 1) * st[a];
+      tapoff += (o[a] - 1) * st;
+      st *= rin;
     }
+    src_t = p.A;
+    off_t = tapoff * p.cin + (row2 - tap * p.cin);
+    xmask_t = -1;
   }
-  // MODE 2: voxel table of chunk c into vtab[c & 1]
-  auto fill_vtab = [&](int c) {
-    if (MODE == 2 && tid < TB_K) {
-      const int v = kbeg + c * TB_K + tid;
-      int2 e = make_int2(0, 0x100);
-      if (c < nch && v < kend) {
-        int s[4], q = v;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          s[a] = (q % rout) * p.stride;
-          q /= rout;
-        }
-        e = make_int2(s[0] + s[1] * is1 + s[2] * is2 + s[3] * is3, edge_mask(s, rin));
-      }
-      vtab[c & 1][tid] = e;
-    }
-  };
-  fill_vtab(0);
+  if (MODE == 2) fill_vtab(vtab[0], tid, kbeg, 0, nch, kend, rout, rin, p.stride, p.cin);
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tacc = tbase;
   const uint32_t idesc = idesc_bf16_f32(TB_M, N);
+  // MODE 0/1 staging: this thread loads 4 channels (half of reduction group
+  // kgl) of rows rsub, rsub + 16, ..., so 16 lanes read 256 contiguous bytes
+  // of a row when the chunk stays within one tap
+  const int half = tid & 1, kgl = (tid >> 1) & 7, rsub = tid >> 4;
+  const int ch = MODE == 0 ? p.cin : p.cout;
 
   int issued = 0;  // chunks whose MMAs were issued (block-uniform)
   bool bad = false;
@@ -190,80 +226,88 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
     unsigned char *Blo = Bhi + N * TB_K * 2;
     if (i >= 2 && !mbar_wait_bounded(&bars[s], ((i - 2) >> 1) & 1)) bad = true;
     if (!bad) {
-      fill_vtab(i + 1);
-      // ---- A: 8 reduction groups of this thread's row
+      if (MODE == 2)
+        fill_vtab(vtab[(i + 1) & 1], tid, kbeg, i + 1, nch, kend, rout, rin, p.stride, p.cin);
+      // ---- A
       if (MODE == 0 || MODE == 1) {
-        float x[8][8];
+        const int k = k0 + kgl * 8 + half * 4;
+        float4 xv[TB_M / 16];
 #pragma unroll
-        for (int kg = 0; kg < 8; ++kg) {
-          const int k = k0 + kg * 8;
+        for (int it = 0; it < TB_M / 16; ++it) xv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (VEC) {
+          if (k < p.K) {
+            const int tap = k / ch, c = k - tap * ch;
+            if (MODE == 0 || mirror) {
+              const TapEnt t = taps[tap];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) x[kg][j] = 0.f;
-          if (VEC) {
-            const int ch = MODE == 0 ? p.cin : p.cout;
-            if (rowvalid && k < p.K) {
-              const int tap = k / ch, c0 = k - tap * ch;
-              const float *src = nullptr;
-              if (MODE == 0) {
-                const TapEnt t = taps[tap];
-                if (!(rowmask & t.need)) src = p.A + (size_t)(rowlin + t.off) * p.cin + c0;
-              } else {
-                int o[4];
-                tap_digits(tap, o);
-                bool ok = true;
+              for (int it = 0; it < TB_M / 16; ++it) {
+                const int2 ri = rows_s[it * 16 + rsub];
+                if (!(ri.y & t.need))
+                  xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)(ri.x + t.off) * ch + c));
+              }
+            } else {  // MODE 1, stride 2
+              int o[4];
+              tap_digits(tap, o);
+#pragma unroll
+              for (int it = 0; it < TB_M / 16; ++it) {
+                const int2 ri = rows_s[it * 16 + rsub];
+                bool ok = ri.y != 0;
                 int lin = 0, mul = 1;
 #pragma unroll
                 for (int a = 0; a < 4; ++a) {
-                  const int num = rc[a] + 1 - o[a];
-                  const int q = num / p.stride;
-                  ok = ok && num >= 0 && q * p.stride == num && q < rout;
+                  const int num = ((ri.x >> (8 * a)) & 255) + 1 - o[a];
+                  const int q = num >> 1;
+                  ok = ok && num >= 0 && (num & 1) == 0 && q < rout;
                   lin += q * mul;
                   mul *= rout;
                 }
-                if (ok) src = p.A + (size_t)lin * p.cout + c0;
-              }
-              if (src) {
-                const float4 u = __ldg(reinterpret_cast<const float4 *>(src));
-                const float4 w = __ldg(reinterpret_cast<const float4 *>(src) + 1);
-                x[kg][0] = u.x, x[kg][1] = u.y, x[kg][2] = u.z, x[kg][3] = u.w;
-                x[kg][4] = w.x, x[kg][5] = w.y, x[kg][6] = w.z, x[kg][7] = w.w;
+                if (ok)
+                  xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)lin * ch + c));
               }
             }
-          } else {  // MODE 0 with a channel count that is not a multiple of 8
+          }
+        } else {  // MODE 0 with a channel count that is not a multiple of 8
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-              const int kj = k + j;
-              if (rowvalid && kj < p.K) {
-                const int tap = kj / p.cin, ci = kj - tap * p.cin;
-                const TapEnt t = taps[tap];
-                if (!(rowmask & t.need))
-                  x[kg][j] = __ldg(p.A + (size_t)(rowlin + t.off) * p.cin + ci);
+          for (int j = 0; j < 4; ++j) {
+            const int kj = k + j;
+            if (kj < p.K) {
+              const int tap = kj / p.cin, ci = kj - tap * p.cin;
+              const TapEnt t = taps[tap];
+#pragma unroll
+              for (int it = 0; it < TB_M / 16; ++it) {
+                const int2 ri = rows_s[it * 16 + rsub];
+                if (!(ri.y & t.need)) {
+                  const float v = __ldg(p.A + (size_t)(ri.x + t.off) * p.cin + ci);
+                  if (j == 0) xv[it].x = v;
+                  if (j == 1) xv[it].y = v;
+                  if (j == 2) xv[it].z = v;
+                  if (j == 3) xv[it].w = v;
+                }
               }
             }
           }
         }
 #pragma unroll
-        for (int kg = 0; kg < 8; ++kg) {
-          uint4 h, l;
-          split8(x[kg], h, l);
-          const uint32_t o = core_off(tid, kg, TB_M);
-          *reinterpret_cast<uint4 *>(Ahi + o) = h;
-          *reinterpret_cast<uint4 *>(Alo + o) = l;
+        for (int it = 0; it < TB_M / 16; ++it) {
+          uint2 h, l;
+          split4(xv[it], h, l);
+          const uint32_t o = swz128(it * 16 + rsub, kgl) + half * 8;
+          *reinterpret_cast<uint2 *>(Ahi + o) = h;
+          *reinterpret_cast<uint2 *>(Alo + o) = l;
         }
       } else {  // MODE 2: row (tap, ci), reduction over voxels
 #pragma unroll
-        for (int kg = 0; kg < 8; ++kg) {
+        for (int g = 0; g < KG_T; ++g) {
+          const int kg = kgbase + g;
           float x[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const int2 e = vtab[s][kg * 8 + j];
-            x[j] = (rowvalid && !(e.y & need_t))
-                       ? __ldg(p.A + (size_t)(e.x + tapoff_t) * p.cin + ci_t)
-                       : 0.f;
+            x[j] = (e.y & need_t) ? 0.f : __ldg(src_t + ((e.x + off_t) & xmask_t));
           }
           uint4 h, l;
           split8(x, h, l);
-          const uint32_t o = core_off(tid, kg, TB_M);
+          const uint32_t o = swz128(lrow, kg);
           *reinterpret_cast<uint4 *>(Ahi + o) = h;
           *reinterpret_cast<uint4 *>(Alo + o) = l;
         }
@@ -280,7 +324,7 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
           }
           uint4 h, l;
           split8(x, h, l);
-          const uint32_t o = core_off(n, kg, N);
+          const uint32_t o = swz128(n, kg);
           *reinterpret_cast<uint4 *>(Bhi + o) = h;
           *reinterpret_cast<uint4 *>(Blo + o) = l;
         } else {
@@ -294,7 +338,7 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
             w = __ldg(reinterpret_cast<const uint4 *>(
                 p.Bw + ((size_t)tap * p.cin + n) * p.cout + c0));
           }
-          *reinterpret_cast<uint4 *>(Bhi + core_off(n, kg, N)) = w;
+          *reinterpret_cast<uint4 *>(Bhi + swz128(n, kg)) = w;
         }
       }
       fence_proxy_async_smem();
@@ -306,13 +350,12 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
       const uint32_t b_hi = smem_addr(Bhi), b_lo = smem_addr(Blo);
 #pragma unroll
       for (int kk = 0; kk < TB_K / 16; ++kk) {
-        const uint32_t ao = kk * 2 * (TB_M * 16), bo = kk * 2 * (N * 16);
-        const uint64_t dah = smem_desc(a_hi + ao, TB_M * 16, 128);
-        const uint64_t dal = smem_desc(a_lo + ao, TB_M * 16, 128);
-        const uint64_t dbh = smem_desc(b_hi + bo, N * 16, 128);
+        const uint64_t dah = smem_desc_sw128(a_hi + kk * 32);
+        const uint64_t dal = smem_desc_sw128(a_lo + kk * 32);
+        const uint64_t dbh = smem_desc_sw128(b_hi + kk * 32);
         mma_bf16(tacc, dah, dbh, idesc, (i | kk) != 0);
         mma_bf16(tacc, dal, dbh, idesc, 1);
-        if (MODE == 2) mma_bf16(tacc, dah, smem_desc(b_lo + bo, N * 16, 128), idesc, 1);
+        if (MODE == 2) mma_bf16(tacc, dah, smem_desc_sw128(b_lo + kk * 32), idesc, 1);
       }
       mma_commit(&bars[s]);
     }
@@ -329,12 +372,15 @@ __global__ void __launch_bounds__(TB_T) k_conv_tc(TcArgs p) {
   ok = __syncthreads_and(ok) && issued > 0;
   fence_after_sync();
   if (ok) {
-    const int r = m0 + 32 * warp + (tid & 31);
+    // warp w reads tensor-memory lanes 32 (w % 4) .. + 31; warps 0-3 and
+    // 4-7 take alternate 16-column groups
+    const int q4 = warp & 3;
+    const int r = m0 + 32 * q4 + (tid & 31);
     const bool split = MODE == 2 || gridDim.z > 1;
     float *C = p.C + (split ? (size_t)blockIdx.z * p.M * N : 0);
-    for (int c0 = 0; c0 < N; c0 += 16) {
+    for (int c0 = 16 * (warp >> 2); c0 < N; c0 += 32) {
       float v[16];
-      tmem_ld16(tacc + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+      tmem_ld16(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0, v);
       if (r < p.M) {
         if (!split && MODE == 0) {
 #pragma unroll
@@ -373,37 +419,105 @@ __global__ void k_sum_slices_epi(const float *__restrict__ work, float *__restri
 }
 
 // BF16 copies of one layer's weights W[tap][ci][co]: WB in the same order,
-// WT[co][tap * cin + ci] with rows of length kpad (the tail stays zero)
+// WT[co][tap * cin + ci] with rows of length kpad (the tail stays zero).
+// Both loops write consecutive entries from consecutive threads.
 __global__ void k_weights_tc(const float *__restrict__ wq, uint16_t *__restrict__ wb,
                              uint16_t *__restrict__ wt, int taps, int cin, int cout, int kpad) {
-  const long long n = (long long)taps * cin * cout;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x) {
-    const __nv_bfloat16 b = __float2bfloat16_rn(wq[q]);
-    const uint16_t bits = *reinterpret_cast<const uint16_t *>(&b);
-    const int co = (int)(q % cout);
-    const long long k = q / cout;  // tap * cin + ci
-    wb[q] = bits;
-    wt[(size_t)co * kpad + k] = bits;
+  const long long K = (long long)taps * cin, n = K * cout;
+  const long long step = (long long)gridDim.x * blockDim.x;
+  auto bits = [](float x) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(x);
+    return *reinterpret_cast<const uint16_t *>(&b);
+  };
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += step)
+    wb[q] = bits(wq[q]);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += step) {
+    const long long co = q / K, k = q - co * K;
+    wt[(size_t)co * kpad + k] = bits(wq[(size_t)k * cout + co]);
   }
+}
+
+// Weight and bias gradient of a 1^4 convolution with CI inputs and CO
+// outputs: each thread accumulates its voxels' products, the block reduces
+// them in a fixed order into part[block][CI CO + CO].
+template <int CI, int CO>
+__global__ void __launch_bounds__(256) k_wgrad_1x1(const float *__restrict__ in,
+                                                   const float *__restrict__ dout, long long V,
+                                                   float *__restrict__ part) {
+  constexpr int NV = CI * CO + CO;
+  __shared__ float red[8][NV];
+  float acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) acc[j] = 0.f;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V;
+       v += (long long)gridDim.x * blockDim.x) {
+    float a[CI], d[CO];
+#pragma unroll
+    for (int c = 0; c < CI; ++c) a[c] = __ldg(in + v * CI + c);
+#pragma unroll
+    for (int c = 0; c < CO; ++c) d[c] = __ldg(dout + v * CO + c);
+#pragma unroll
+    for (int ci = 0; ci < CI; ++ci)
+#pragma unroll
+      for (int co = 0; co < CO; ++co) acc[ci * CO + co] += a[ci] * d[co];
+#pragma unroll
+    for (int co = 0; co < CO; ++co) acc[CI * CO + co] += d[co];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    float x = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][j] = x;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < NV; j += blockDim.x) {
+    float x = 0.f;
+    for (int w = 0; w < 8; ++w) x += red[w][j];
+    part[(size_t)blockIdx.x * NV + j] = x;
+  }
+}
+
+// out[j] = sum over the blocks' partials: one warp per entry, lane l adds
+// blocks l, l + 32, ... in order, then a fixed butterfly (deterministic)
+__global__ void k_sum_parts(const float *__restrict__ part, int nblocks, int nv,
+                            float *__restrict__ out) {
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (j >= nv) return;
+  float x = 0.f;
+  for (int b = lane; b < nblocks; b += 32) x += part[(size_t)b * nv + j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if (lane == 0) out[j] = x;
 }
 
 struct TcPlan {
   int nz, kslice;
 };
 
-// Slices of the reduction: about two blocks per SM in total, at least four
-// chunks per slice.
-TcPlan tc_plan(long long M, long long K) {
+// Slices of the reduction.  With `slots` = resident blocks per SM x SMs, a
+// split into nz slices takes ceil(tiles nz / slots) waves of ceil(chunks /
+// nz) chunks each, plus the pass that sums the slices: a launch (about 1.5
+// chunk times) and reading nz M N floats (about 1.1 M of them per chunk
+// time).  The split with the lowest estimate wins (at least four chunks per
+// slice).
+TcPlan tc_plan(long long M, long long K, int N, int resident) {
   const long long tiles = (M + TB_M - 1) / TB_M;
   const long long chunks = (K + TB_K - 1) / TB_K;
-  const long long target = 2LL * sm_count();
-  long long nz = tiles >= target ? 1 : (target + tiles - 1) / tiles;
-  const long long maxz = chunks / 4 > 1 ? chunks / 4 : 1;
-  if (nz > maxz) nz = maxz;
-  long long per = (chunks + nz - 1) / nz;
-  nz = (chunks + per - 1) / per;
-  return TcPlan{(int)nz, (int)(per * TB_K)};
+  const long long slots = (long long)std::max(resident, 1) * sm_count();
+  const long long maxz = std::max(chunks / 4, 1LL);
+  long long best = 1;
+  double best_t = 1e300;
+  for (long long nz = 1; nz <= maxz; ++nz) {
+    const long long per = (chunks + nz - 1) / nz;
+    const long long z = (chunks + per - 1) / per;  // slices actually used
+    const long long waves = (tiles * z + slots - 1) / slots;
+    const double t = (double)(waves * per) + (z > 1 ? 1.5 + (double)z * M * N / 1.1e6 : 0.0);
+    if (t < best_t) best_t = t, best = z;
+  }
+  const long long per = (chunks + best - 1) / best;
+  return TcPlan{(int)((chunks + per - 1) / per), (int)(per * TB_K)};
 }
 
 int pow2_cols(int n) {
@@ -412,18 +526,46 @@ int pow2_cols(int n) {
   return c;
 }
 
+template <int MODE>
+int tc_smem(int N) {
+  return 2 * (2 * A_TILE + (MODE == 2 ? 2 : 1) * N * TB_K * 2) + 1024;
+}
+
+// once per kernel: room for the largest stage pair (N = 128, two B tiles)
+template <int MODE, int VEC>
+void tc_attr() {
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_conv_tc<MODE, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           tc_smem<2>(128));
+  fh::cuda_check(attr, "cudaFuncSetAttribute(k_conv_tc)");
+}
+
+template <int MODE, int VEC>
+int tc_resident(int N) {
+  tc_attr<MODE, VEC>();
+  int nb = 0;
+  fh::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<MODE, VEC>, TB_T,
+                                                               tc_smem<MODE>(N)),
+                 "cudaOccupancyMaxActiveBlocksPerMultiprocessor(k_conv_tc)");
+  return nb;
+}
+
+template <int MODE, int VEC>
+TcPlan tc_plan_for(long long M, long long K, int N) {
+  return tc_plan(M, K, N, tc_resident<MODE, VEC>(N));
+}
+
 template <int MODE, int VEC>
 void launch_tc(const TcArgs &a0, int nz, cudaStream_t s) {
   TcArgs a = a0;
   a.ncols = pow2_cols(a.N);
-  const int smem = 2 * (2 * A_TILE + (MODE == 2 ? 2 : 1) * a.N * TB_K * 2);
-  // once per kernel: room for the largest stage pair (N = 128, two B tiles)
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      k_conv_tc<MODE, VEC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      2 * (2 * A_TILE + 2 * 128 * TB_K * 2));
-  fh::cuda_check(attr, "cudaFuncSetAttribute(k_conv_tc)");
+  tc_attr<MODE, VEC>();
   dim3 grid((a.M + TB_M - 1) / TB_M, 1, nz);
-  k_conv_tc<MODE, VEC><<<grid, TB_T, smem, s>>>(a);
+  k_conv_tc<MODE, VEC><<<grid, TB_T, tc_smem<MODE>(a.N), s>>>(a);
+}
+
+TcPlan plan_fwd(long long M, long long K, int cin, int cout) {
+  return cin % 8 == 0 ? tc_plan_for<0, 1>(M, K, cout) : tc_plan_for<0, 0>(M, K, cout);
 }
 
 }  // namespace
@@ -450,18 +592,28 @@ size_t net_tc_work(int rin, int rout, int cin, int cout, int ks) {
   size_t w = 0;
   const long long Vi = (long long)rin * rin * rin * rin, Vo = (long long)rout * rout * rout * rout;
   if (net_tc_fwd_ok(cin, cout, ks)) {
-    const TcPlan pl = tc_plan(Vo, net_tc_kpad(cin, ks));
+    const TcPlan pl = plan_fwd(Vo, net_tc_kpad(cin, ks), cin, cout);
     if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vo * cout);
   }
   if (net_tc_bwd_data_ok(cin, cout, ks)) {
-    const TcPlan pl = tc_plan(Vi, 81LL * cout);
+    const TcPlan pl = tc_plan_for<1, 1>(Vi, 81LL * cout, cin);
     if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vi * cin);
   }
   if (net_tc_bwd_weight_ok(cin, cout, ks)) {
-    const TcPlan pl = tc_plan(81LL * cin, Vo);
-    w = std::max(w, (size_t)pl.nz * 81 * cin * cout);
+    const TcPlan pl = tc_plan_for<2, 0>(81LL * cin + 1, Vo, cout);
+    w = std::max(w, (size_t)pl.nz * (81 * cin + 1) * cout);
   }
   return w;
+}
+
+bool net_wgrad_1x1_ok(int cin, int cout, int ks) { return ks == 1 && cin == 16 && cout == 4; }
+size_t net_wgrad_1x1_work() { return (size_t)2 * 152 * (16 * 4 + 4) * 4; }
+
+void net_wgrad_1x1(const float *in, const float *dout, float *dw, float *work, long long V,
+                   cudaStream_t s) {
+  const int nb = std::min(2 * sm_count(), 4 * 152);
+  k_wgrad_1x1<16, 4><<<nb, 256, 0, s>>>(in, dout, V, work);
+  k_sum_parts<<<(16 * 4 + 4 + 3) / 4, 128, 0, s>>>(work, nb, 16 * 4 + 4, dw);
 }
 
 void net_weights_tc(const float *wq, uint16_t *wb, uint16_t *wt, int cin, int cout, int ks,
@@ -485,7 +637,7 @@ void net_tc_conv_fwd(const float *in, const uint16_t *wt, const float *b, float 
   a.K = 81 * cin;
   a.Kpad = net_tc_kpad(cin, 3);
   a.relu = relu;
-  const TcPlan pl = tc_plan(a.M, a.Kpad);
+  const TcPlan pl = plan_fwd(a.M, a.Kpad, cin, cout);
   a.kslice = pl.kslice;
   a.bias = pl.nz > 1 ? nullptr : b;
   a.C = pl.nz > 1 ? work : out;
@@ -511,7 +663,7 @@ void net_tc_conv_bwd_data(const float *dout, const uint16_t *wb, float *din, flo
   a.N = cin;
   a.K = 81 * cout;
   a.Kpad = a.K;
-  const TcPlan pl = tc_plan(a.M, a.K);
+  const TcPlan pl = tc_plan_for<1, 1>(a.M, a.K, a.N);
   a.kslice = pl.kslice;
   a.C = pl.nz > 1 ? work : din;
   launch_tc<1, 1>(a, pl.nz, s);
@@ -528,11 +680,12 @@ void net_tc_conv_bwd_weight(const float *in, const float *dout, float *dw, float
   a.B32 = dout;
   a.err = err;
   a.rin = rin, a.rout = rout, a.cin = cin, a.cout = cout, a.stride = stride;
-  a.M = 81 * cin;
+  a.M = 81 * cin + 1;  // the (tap, ci) rows and the bias row
+  a.bias_row = 1;
   a.N = cout;
   a.K = rout * rout * rout * rout;
   a.Kpad = a.K;
-  const TcPlan pl = tc_plan(a.M, a.K);
+  const TcPlan pl = tc_plan_for<2, 0>(a.M, a.K, a.N);
   a.kslice = pl.kslice;
   a.C = work;
   launch_tc<2, 0>(a, pl.nz, s);

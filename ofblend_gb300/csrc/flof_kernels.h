@@ -311,6 +311,15 @@ void net_tc_conv_fwd(const float *in, const uint16_t *wt, const float *b, float 
 void net_tc_conv_bwd_data(const float *dout, const uint16_t *wb, float *din, float *work,
                           int rin, int rout, int cin, int cout, int stride, int *err,
                           cudaStream_t s);
+// Weight and bias gradient of the 1^4 output layer (16 -> 4 channels) over
+// V voxels: dw receives the 64 weight entries then the 4 bias entries; work
+// holds net_wgrad_1x1_work() floats.
+bool net_wgrad_1x1_ok(int cin, int cout, int ks);
+size_t net_wgrad_1x1_work();
+void net_wgrad_1x1(const float *in, const float *dout, float *dw, float *work, long long V,
+                   cudaStream_t s);
+// dw receives 81 cin cout weight-gradient entries followed by the cout bias
+// gradients
 void net_tc_conv_bwd_weight(const float *in, const float *dout, float *dw, float *work, int rin,
                             int rout, int cin, int cout, int stride, int *err, cudaStream_t s);
 

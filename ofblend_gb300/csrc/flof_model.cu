@@ -118,15 +118,21 @@ void layer_bwd(flof_model *m, int l, const float *in, const float *dy, float *di
   const int R = m->R;
   cudaStream_t s = S(m);
   const int rin = R / L.rin_div, rout = R / L.rout_div;
-  if (net_tc_bwd_weight_ok(L.cin, L.cout, L.ks))
+  if (net_wgrad_1x1_ok(L.cin, L.cout, L.ks)) {
+    net_wgrad_1x1(in, dy, m->scratch, m->work, (long long)rout * rout * rout * rout, s);
+    net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l] + L.cout, s);
+  } else if (net_tc_bwd_weight_ok(L.cin, L.cout, L.ks)) {
+    // weights and bias in one pass; the bias follows the weights in grad
     net_tc_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.stride,
                            E(m), s);
-  else
+    net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l] + L.cout, s);
+  } else {
     net_conv_bwd_weight(in, dy, m->scratch, m->work, rin, rout, L.cin, L.cout, L.ks, L.stride,
                         s);
-  net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l], s);
-  net_bias_grad(dy, m->scratch, (long long)rout * rout * rout * rout, L.cout, s);
-  net_add_into(m->grad + m->boff[l], m->scratch, L.cout, s);
+    net_add_into(m->grad + m->woff[l], m->scratch, m->wsize[l], s);
+    net_bias_grad(dy, m->scratch, (long long)rout * rout * rout * rout, L.cout, s);
+    net_add_into(m->grad + m->boff[l], m->scratch, L.cout, s);
+  }
   if (!din) return;
   if (net_tc_bwd_data_ok(L.cin, L.cout, L.ks))
     net_tc_conv_bwd_data(dy, m->wb + m->woff[l], din, m->work, rin, rout, L.cin, L.cout,
@@ -216,14 +222,14 @@ FLOF_API int flof_model_create(flof_ctx *c, int res, flof_model **out) {
     m->grad = m->alloc(off);
     m->m = m->alloc(off);
     m->v = m->alloc(off);
-    m->scratch = m->alloc(maxw);
+    m->scratch = m->alloc(maxw + 128);  // a weight gradient and its bias gradient
     size_t maxwork = 0;
     long long wtsize = 0;
     for (int l = 0; l < 8; ++l) {
       const LayerDef &L = LAYERS[l];
       const size_t wk = net_conv_bwd_weight_work(res / L.rout_div, L.cin, L.cout, L.ks);
       const size_t wt = net_tc_work(res / L.rin_div, res / L.rout_div, L.cin, L.cout, L.ks);
-      maxwork = std::max(maxwork, std::max(wk, wt));
+      maxwork = std::max(maxwork, std::max(std::max(wk, wt), net_wgrad_1x1_work()));
       m->wtoff[l] = wtsize;
       wtsize += (long long)L.cout * net_tc_kpad(L.cin, L.ks);
     }

@@ -5,14 +5,20 @@
 // epilogue.  Written from the PTX ISA's description of these instructions
 // for sm_100a / sm_103a.
 //
-// Operand layout in shared memory (no swizzle, K-major): an operand tile of
-// R rows (R a multiple of 8) and 64 reduction entries is a grid of 8-row x
-// 16-byte core matrices.  Core matrix (row group g, reduction group c) sits
-// at byte (c * R / 8 + g) * 128 of the tile, its row r at + 16 r, so the
-// 8 BF16 values of one (row, reduction group) are one 16-byte store.  In the
-// matrix descriptor the leading-dimension offset is the distance between
-// core matrices adjacent along the reduction (R * 16 bytes) and the stride
-// offset the distance between adjacent row groups (128 bytes).
+// Operand layouts in shared memory (K-major: each row's reduction entries
+// are contiguous in 16-byte chunks of 8 BF16 values):
+//  - no swizzle: a tile of R rows (R a multiple of 8) and 64 reduction
+//    entries is a grid of 8-row x 16-byte core matrices; core matrix (row
+//    group g, reduction group c) sits at byte (c * R / 8 + g) * 128, its row r
+//    at + 16 r.  Leading-dimension offset R * 16 bytes (between core matrices
+//    adjacent along the reduction), stride offset 128 bytes (between row
+//    groups).
+//  - 128-byte swizzle: row r's 64 entries form one 128-byte line at
+//    (r / 8) * 1024 + (r % 8) * 128, its 16-byte chunk c stored at position
+//    c ^ (r % 8).  Stride offset 1024 bytes (between 8-row groups); the tile
+//    starts on a 1024-byte boundary; the K = 16 step kk starts at + 32 kk.
+//    A warp writing the 8 chunks of a row, or one chunk of 8 rows, meets no
+//    bank conflict.
 #pragma once
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -36,6 +42,16 @@ __device__ __forceinline__ uint32_t core_off(int row, int kg, int rows) {
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Descriptor of a 128-byte-swizzled K-major tile (layout type 2 in bits
+// 61-63, stride offset 1024 bytes; the leading offset is not used)
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         (1ull << 46) | (2ull << 61);
+}
+__device__ __forceinline__ uint32_t swz128(int row, int chunk) {
+  return (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + ((chunk ^ (row & 7)) << 4));
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
@@ -135,6 +151,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
   const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<const uint32_t *>(&h);
+}
+__device__ __forceinline__ void split4(const float4 &x, uint2 &hi, uint2 &lo) {
+  const float h0 = __bfloat162float(__float2bfloat16_rn(x.x));
+  const float h1 = __bfloat162float(__float2bfloat16_rn(x.y));
+  const float h2 = __bfloat162float(__float2bfloat16_rn(x.z));
+  const float h3 = __bfloat162float(__float2bfloat16_rn(x.w));
+  hi = make_uint2(pack_bf16(h0, h1), pack_bf16(h2, h3));
+  lo = make_uint2(pack_bf16(__fsub_rn(x.x, h0), __fsub_rn(x.y, h1)),
+                  pack_bf16(__fsub_rn(x.z, h2), __fsub_rn(x.w, h3)));
 }
 __device__ __forceinline__ void split8(const float (&x)[8], uint4 &hi, uint4 &lo) {
   float h[8], l[8];
