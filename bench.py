@@ -142,6 +142,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_tflops():
+    """Burst cuBLAS bf16 TFLOP/s of this GPU (the tensor roofline)."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes (read + write) of the kernel classes measured by
     ncu at 64^4, from the committed summary's table (profiles/)."""
@@ -635,6 +646,12 @@ def net_flops(res: int) -> float:
     return float(sum(2 * taps * ci * co * (res // div) ** 4 for ci, co, taps, div in layers))
 
 
+def net_train_flops(res: int) -> float:
+    """FLOPs of one training sample: forward, weight gradients, and input
+    gradients of every layer but the first."""
+    return 3.0 * net_flops(res) - 2.0 * 81 * 2 * 16 * res ** 4
+
+
 def run_learned(a):
     """The learned warm start: trained on the GPU from plain-solver outputs of
     seeded 1-3 drop pairs at 32^4, then the two-way deformations of the
@@ -682,13 +699,14 @@ def run_learned(a):
                      "cg_iterations": [x["cg_total_iterations"] for x in st],
                      "warm_start": [x["warm_start"] for x in st],
                      "coarse_err_zero_vs_pred": [x["warm_start_err"] for x in st]}
-    fl = net_flops(16)
     nsamp = a.train_pairs * a.train_epochs
     line = {
         "metric": f"4D flow solves/s at {R}^4 to fixed residual: learned warm-start vs plain CG",
         "value": res["warm"]["solves_per_s"], "unit": UNIT, "n_gpus": 1, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": res["warm"]["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (network: bf16 weights, f32 accumulate)",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (network: tcgen05 bf16 MMAs, activations and gradients as bf16 hi/lo pairs, "
+                 "f32 accumulation in tensor memory)",
         "data": "synthetic (training: seeded 1-3 drop pairs at 32^4; evaluation: data 0 <-> 1)",
         "config": {"workload": f"both deformations at {R}^4, flof parameters, cgAccuracy {a.cg_accuracy}",
                    "train_pairs": a.train_pairs, "train_epochs": a.train_epochs},
@@ -697,8 +715,17 @@ def run_learned(a):
         "training": {"data_seconds": round(t_data, 2), "train_seconds": round(t_train, 2),
                      "loss_first_last": [round(hist[0], 6), round(hist[-1], 6)],
                      "samples_per_s": round(nsamp / t_train, 1),
-                     "net_tflops_fwd_bwd": round(3 * fl * nsamp / t_train / 1e12, 3)},
+                     "net_tflops_fwd_bwd": round(net_train_flops(16) * nsamp / t_train / 1e12, 3)},
     }
+    pk, pk_kind = measured_bf16_tflops()
+    ach = net_train_flops(16) * nsamp / t_train / 1e12
+    # training throughput in useful network FLOPs (2 x 81 x cin x cout per
+    # output voxel and 3^4 layer; forward, weight and input gradients)
+    # against the bf16 tensor peak
+    line["roofline"] = {"bound": "tensor", "region": "network training (whole train loop)",
+                        "achieved": round(ach, 3), "peak": pk, "unit": "TFLOP/s",
+                        "frac": round(ach / pk, 5), "traffic": None,
+                        "peak_source": f"bf16_tflops of {pk_kind}"}
     print(json.dumps(line), flush=True)
     m.detach()
     ctx.close()
