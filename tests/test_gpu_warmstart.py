@@ -61,6 +61,35 @@ def test_gradients_match_finite_differences(gpu):
     assert np.abs(gg - fd).max() <= 2e-3 * scale + 1e-7, np.c_[gg, fd]
 
 
+def test_full_gradient_at_16_matches_oracle(gpu):
+    """At the coarse extent the driver uses (16^4) every tensor-core shape
+    runs: unsplit tiles with the bias and ReLU epilogue, split reductions, the
+    two-channel first layer, stride-2 input gradients.  The forward pass and
+    the whole gradient (every weight and bias) are compared with the oracle's
+    analytic backward pass (itself checked against finite differences)."""
+    R = 16
+    m = F.Model(R, seed=8)
+    p = W.bf16_round(m.get_params())
+    m.set_params(p)
+    i0, i1, tgt = rand_case(R, 3)
+    g0, g1, gt = grids(R, i0, i1, tgt)
+    out = F.Grid4Vec4(dims=(R,) * 4)
+    m.predict(g0, g1, out)
+    want = W.forward(p, i0, i1)
+    assert np.abs(out.to_numpy() - want).max() <= 1e-4 * max(1.0, np.abs(want).max())
+    loss, g = m.loss_grad(g0, g1, gt)
+    wloss, wg = W.loss_and_grad(p, i0, i1, tgt)
+    assert abs(loss - wloss) <= 1e-4 * abs(wloss)
+    off = 0
+    for l, (cin, cout, ks, *_) in enumerate(W.LAYERS):
+        for n in ((81 if ks == 3 else 1) * cin * cout, cout):  # weights, then biases
+            a, b = g[off:off + n].astype(np.float64), wg[off:off + n]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            assert rel <= 1e-3, (l, n, rel)
+            off += n
+    assert off == g.size
+
+
 def test_training_reduces_loss(gpu):
     R = 8
     m = F.Model(R, seed=6)

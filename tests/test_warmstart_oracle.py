@@ -1,6 +1,7 @@
 """CPU checks of the learned warm start's oracle (oracle/warmstart_net.py):
 its vectorised 4D convolution against a direct loop, the parameter count,
-bf16 rounding, and finite differences against a hand-derived gradient."""
+bf16 rounding, finite differences against a hand-derived gradient, and the
+analytic backward pass against finite differences."""
 import numpy as np
 
 from oracle import warmstart_net as W
@@ -54,3 +55,24 @@ def test_fd_gradient_of_output_bias():
     fd = W.fd_grad(p, i0, i1, tgt, idx)
     exact = 2.0 * (pred - tgt).reshape(-1, 4).sum(0) / pred.size
     assert np.allclose(fd, exact, rtol=1e-5, atol=1e-8)
+
+
+def test_analytic_gradient_matches_finite_differences():
+    """loss_and_grad (backpropagation) against central differences of the
+    loss, for parameters of every layer, weights and biases."""
+    r = np.random.default_rng(2)
+    R = 4
+    p = r.standard_normal(W.num_params()) * 0.05
+    i0 = (r.standard_normal((R,) * 4) * 0.004).astype(np.float32)
+    i1 = (r.standard_normal((R,) * 4) * 0.004).astype(np.float32)
+    tgt = (r.standard_normal((R,) * 4 + (4,)) * 0.5).astype(np.float32)
+    loss, g = W.loss_and_grad(p, i0, i1, tgt)
+    assert abs(loss - W.loss(p, i0, i1, tgt)) <= 1e-12 * abs(loss)
+    assert g.shape == (W.num_params(),)
+    idx, off = [], 0
+    for cin, cout, ks, *_ in W.LAYERS:
+        nw = (81 if ks == 3 else 1) * cin * cout
+        idx += list(off + r.choice(nw, 4, replace=False)) + [off + nw + int(r.integers(cout))]
+        off += nw + cout
+    fd = W.fd_grad(p, i0, i1, tgt, idx, rel=1e-4)
+    assert np.abs(g[idx] - fd).max() <= 1e-7 * np.abs(fd).max() + 1e-12
