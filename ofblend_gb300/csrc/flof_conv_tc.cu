@@ -29,6 +29,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "flof_internal.h"
 #include "flof_tcgen05.cuh"
@@ -540,13 +541,21 @@ void tc_attr() {
   fh::cuda_check(attr, "cudaFuncSetAttribute(k_conv_tc)");
 }
 
+// resident blocks per SM for N columns (N a multiple of 16 up to 128),
+// queried once per shape
 template <int MODE, int VEC>
 int tc_resident(int N) {
+  static std::atomic<int> cache[128 / 16 + 1];
+  std::atomic<int> &slot = cache[N / 16];
+  const int known = slot.load(std::memory_order_relaxed);
+  if (known > 0) return known;
   tc_attr<MODE, VEC>();
   int nb = 0;
   fh::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<MODE, VEC>, TB_T,
                                                                tc_smem<MODE>(N)),
                  "cudaOccupancyMaxActiveBlocksPerMultiprocessor(k_conv_tc)");
+  nb = std::max(nb, 1);
+  slot.store(nb, std::memory_order_relaxed);
   return nb;
 }
 
