@@ -108,6 +108,81 @@ __device__ __forceinline__ void fill_vtab(int2 *vt, int tid, int kbeg, int c, in
   vt[tid] = e;
 }
 
+// MODE 0/1 gather: this thread's four channels, starting at reduction index
+// k, of rows rsub, rsub + 16, ... of the tile (zero where the tap falls
+// outside the grid or k is past the end)
+template <int MODE, int VEC>
+__device__ __forceinline__ void gather01(float4 (&xv)[TB_M / 16], const TcArgs &p, int k,
+                                         const TapEnt *taps, const int2 *rows_s, int rsub,
+                                         bool mirror, int ch) {
+#pragma unroll
+  for (int it = 0; it < TB_M / 16; ++it) xv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (VEC) {
+    if (k >= p.K) return;
+    const int tap = k / ch, c = k - tap * ch;
+    if (MODE == 0 || mirror) {
+      const TapEnt t = taps[tap];
+#pragma unroll
+      for (int it = 0; it < TB_M / 16; ++it) {
+        const int2 ri = rows_s[it * 16 + rsub];
+        if (!(ri.y & t.need))
+          xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)(ri.x + t.off) * ch + c));
+      }
+    } else {  // MODE 1, stride 2
+      int o[4];
+      tap_digits(tap, o);
+#pragma unroll
+      for (int it = 0; it < TB_M / 16; ++it) {
+        const int2 ri = rows_s[it * 16 + rsub];
+        bool ok = ri.y != 0;
+        int lin = 0, mul = 1;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          const int num = ((ri.x >> (8 * a)) & 255) + 1 - o[a];
+          const int q = num >> 1;
+          ok = ok && num >= 0 && (num & 1) == 0 && q < p.rout;
+          lin += q * mul;
+          mul *= p.rout;
+        }
+        if (ok) xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)lin * ch + c));
+      }
+    }
+  } else {  // MODE 0 with a channel count that is not a multiple of 8
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int kj = k + j;
+      if (kj < p.K) {
+        const int tap = kj / p.cin, ci = kj - tap * p.cin;
+        const TapEnt t = taps[tap];
+#pragma unroll
+        for (int it = 0; it < TB_M / 16; ++it) {
+          const int2 ri = rows_s[it * 16 + rsub];
+          if (!(ri.y & t.need)) {
+            const float v = __ldg(p.A + (size_t)(ri.x + t.off) * p.cin + ci);
+            if (j == 0) xv[it].x = v;
+            if (j == 1) xv[it].y = v;
+            if (j == 2) xv[it].z = v;
+            if (j == 3) xv[it].w = v;
+          }
+        }
+      }
+    }
+  }
+}
+
+// MODE 2 gather: this thread's row over the 8 voxels of each of its KG_T
+// reduction groups (voxel table vt of the chunk)
+__device__ __forceinline__ void gather2(float (&xw)[KG_T][8], const int2 *vt, int kgbase,
+                                        int need_t, const float *src_t, int off_t, int xmask_t) {
+#pragma unroll
+  for (int g = 0; g < KG_T; ++g)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int2 e = vt[(kgbase + g) * 8 + j];
+      xw[g][j] = (e.y & need_t) ? 0.f : __ldg(src_t + ((e.x + off_t) & xmask_t));
+    }
+}
+
 template <int MODE, int VEC>
 __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   extern __shared__ unsigned char smem_raw[];
@@ -115,7 +190,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   __shared__ uint32_t tbase;
   __shared__ TapEnt taps[81];     // MODE 0, and MODE 1 at stride 1
   __shared__ int2 rows_s[TB_M];   // MODE 0/1: row table (see below)
-  __shared__ int2 vtab[2][TB_K];  // MODE 2: voxel tables of two chunks
+  __shared__ int2 vtab[3][TB_K];  // MODE 2: voxel tables of three chunks
 
   // tiles start on 1024-byte boundaries (128-byte swizzle)
   unsigned char *smem = smem_raw + ((1024u - (smem_addr(smem_raw) & 1023u)) & 1023u);
@@ -204,7 +279,10 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     off_t = tapoff * p.cin + (row2 - tap * p.cin);
     xmask_t = -1;
   }
-  if (MODE == 2) fill_vtab(vtab[0], tid, kbeg, 0, nch, kend, rout, rin, p.stride, p.cin);
+  if (MODE == 2) {
+    fill_vtab(vtab[0], tid, kbeg, 0, nch, kend, rout, rin, p.stride, p.cin);
+    fill_vtab(vtab[1], tid, kbeg, 1, nch, kend, rout, rin, p.stride, p.cin);
+  }
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   fence_before_sync();
   __syncthreads();
@@ -217,6 +295,16 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   const int half = tid & 1, kgl = (tid >> 1) & 7, rsub = tid >> 4;
   const int ch = MODE == 0 ? p.cin : p.cout;
 
+  // The next chunk's A values are loaded into registers right after this
+  // chunk's are stored, so the loads are in flight across the barrier, the
+  // MMA issue and the next stage's wait.
+  float4 xv[TB_M / 16];  // MODE 0/1
+  float xw[KG_T][8];     // MODE 2
+  if (MODE == 2)
+    gather2(xw, vtab[0], kgbase, need_t, src_t, off_t, xmask_t);
+  else
+    gather01<MODE, VEC>(xv, p, kbeg + kgl * 8 + half * 4, taps, rows_s, rsub, mirror, ch);
+
   int issued = 0;  // chunks whose MMAs were issued (block-uniform)
   bool bad = false;
   for (int i = 0; i < nch; ++i) {
@@ -228,66 +316,9 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     if (i >= 2 && !mbar_wait_bounded(&bars[s], ((i - 2) >> 1) & 1)) bad = true;
     if (!bad) {
       if (MODE == 2)
-        fill_vtab(vtab[(i + 1) & 1], tid, kbeg, i + 1, nch, kend, rout, rin, p.stride, p.cin);
-      // ---- A
+        fill_vtab(vtab[(i + 2) % 3], tid, kbeg, i + 2, nch, kend, rout, rin, p.stride, p.cin);
+      // ---- A: store this chunk's registers
       if (MODE == 0 || MODE == 1) {
-        const int k = k0 + kgl * 8 + half * 4;
-        float4 xv[TB_M / 16];
-#pragma unroll
-        for (int it = 0; it < TB_M / 16; ++it) xv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (VEC) {
-          if (k < p.K) {
-            const int tap = k / ch, c = k - tap * ch;
-            if (MODE == 0 || mirror) {
-              const TapEnt t = taps[tap];
-#pragma unroll
-              for (int it = 0; it < TB_M / 16; ++it) {
-                const int2 ri = rows_s[it * 16 + rsub];
-                if (!(ri.y & t.need))
-                  xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)(ri.x + t.off) * ch + c));
-              }
-            } else {  // MODE 1, stride 2
-              int o[4];
-              tap_digits(tap, o);
-#pragma unroll
-              for (int it = 0; it < TB_M / 16; ++it) {
-                const int2 ri = rows_s[it * 16 + rsub];
-                bool ok = ri.y != 0;
-                int lin = 0, mul = 1;
-#pragma unroll
-                for (int a = 0; a < 4; ++a) {
-                  const int num = ((ri.x >> (8 * a)) & 255) + 1 - o[a];
-                  const int q = num >> 1;
-                  ok = ok && num >= 0 && (num & 1) == 0 && q < rout;
-                  lin += q * mul;
-                  mul *= rout;
-                }
-                if (ok)
-                  xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)lin * ch + c));
-              }
-            }
-          }
-        } else {  // MODE 0 with a channel count that is not a multiple of 8
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int kj = k + j;
-            if (kj < p.K) {
-              const int tap = kj / p.cin, ci = kj - tap * p.cin;
-              const TapEnt t = taps[tap];
-#pragma unroll
-              for (int it = 0; it < TB_M / 16; ++it) {
-                const int2 ri = rows_s[it * 16 + rsub];
-                if (!(ri.y & t.need)) {
-                  const float v = __ldg(p.A + (size_t)(ri.x + t.off) * p.cin + ci);
-                  if (j == 0) xv[it].x = v;
-                  if (j == 1) xv[it].y = v;
-                  if (j == 2) xv[it].z = v;
-                  if (j == 3) xv[it].w = v;
-                }
-              }
-            }
-          }
-        }
 #pragma unroll
         for (int it = 0; it < TB_M / 16; ++it) {
           uint2 h, l;
@@ -296,19 +327,12 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
           *reinterpret_cast<uint2 *>(Ahi + o) = h;
           *reinterpret_cast<uint2 *>(Alo + o) = l;
         }
-      } else {  // MODE 2: row (tap, ci), reduction over voxels
+      } else {
 #pragma unroll
         for (int g = 0; g < KG_T; ++g) {
-          const int kg = kgbase + g;
-          float x[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int2 e = vtab[s][kg * 8 + j];
-            x[j] = (e.y & need_t) ? 0.f : __ldg(src_t + ((e.x + off_t) & xmask_t));
-          }
           uint4 h, l;
-          split8(x, h, l);
-          const uint32_t o = swz128(lrow, kg);
+          split8(xw[g], h, l);
+          const uint32_t o = swz128(lrow, kgbase + g);
           *reinterpret_cast<uint4 *>(Ahi + o) = h;
           *reinterpret_cast<uint4 *>(Alo + o) = l;
         }
@@ -341,6 +365,14 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
           }
           *reinterpret_cast<uint4 *>(Bhi + swz128(n, kg)) = w;
         }
+      }
+      // ---- A: the next chunk's loads
+      if (i + 1 < nch) {
+        if (MODE == 2)
+          gather2(xw, vtab[(i + 1) % 3], kgbase, need_t, src_t, off_t, xmask_t);
+        else
+          gather01<MODE, VEC>(xv, p, k0 + TB_K + kgl * 8 + half * 4, taps, rows_s, rsub,
+                              mirror, ch);
       }
       fence_proxy_async_smem();
     }
