@@ -603,6 +603,8 @@ void launch_tc(const TcArgs &a0, int nz, cudaStream_t s) {
   tc_attr<MODE, VEC>();
   dim3 grid((a.M + TB_M - 1) / TB_M, 1, nz);
   k_conv_tc<MODE, VEC><<<grid, TB_T, tc_smem<MODE>(a.N), s>>>(a);
+  // a refused launch (configuration) is reported here, not by a later sync
+  fh::cuda_check(cudaGetLastError(), "k_conv_tc launch");
 }
 
 TcPlan plan_fwd(long long M, long long K, int cin, int cout) {

@@ -183,6 +183,7 @@ namespace fh {
 // The warm start's prediction for the coarsest level (used by the driver).
 void model_predict_raw(flof_model *m, const float *i0, const float *i1, float4 *vel) {
   forward(m, i0, i1, (float *)vel);
+  CK(cudaGetLastError());
 }
 int model_res(const flof_model *m) { return m->R; }
 void model_orphan(flof_model *m) {
@@ -351,6 +352,7 @@ FLOF_API int flof_model_predict(flof_model *m, const flof_grid *i0, const flof_g
     need_model_grid(m, vel, FLOF_VEC4, "vel");
     set_ctx_device(m->ctx);
     forward(m, i0->f(), i1->f(), vel->f());
+    CK(cudaGetLastError());  // a refused launch of any network kernel
     CK(cudaStreamSynchronize(S(m)));
     check_device_errors(m->ctx);
   });
@@ -375,6 +377,7 @@ FLOF_API int flof_model_loss_grad(flof_model *m, const flof_grid *i0, const flof
     if (grad_host)
       CK(cudaMemcpyAsync(grad_host, m->grad, m->nparams * sizeof(float), cudaMemcpyDeviceToHost,
                          S(m)));
+    CK(cudaGetLastError());  // a refused launch of any network kernel
     CK(cudaStreamSynchronize(S(m)));
     check_device_errors(m->ctx);
     if (loss) *loss = *m->hloss;
@@ -406,6 +409,7 @@ FLOF_API int flof_model_train_step(flof_model *m, int n, const flof_grid *const 
     net_adam(m->w, m->wq, m->grad, m->m, m->v, m->nparams, lr, m->step, 1.f / n, S(m));
     refresh_tc_weights(m);
     CK(cudaMemcpyAsync(m->hloss, m->dloss, sizeof(double), cudaMemcpyDeviceToHost, S(m)));
+    CK(cudaGetLastError());  // a refused launch of any network kernel
     CK(cudaStreamSynchronize(S(m)));
     check_device_errors(m->ctx);
     if (loss) *loss = *m->hloss / n;
