@@ -109,56 +109,36 @@ __device__ __forceinline__ void fill_vtab(int2 *vt, int tid, int kbeg, int c, in
 }
 
 // MODE 0/1 gather: this thread's four channels, starting at reduction index
-// k, of rows rsub, rsub + 16, ... of the tile (zero where the tap falls
-// outside the grid or k is past the end)
-template <int MODE, int VEC>
-__device__ __forceinline__ void gather01(float4 (&xv)[TB_M / 16], const TcArgs &p, int k,
-                                         const TapEnt *taps, const int2 *rows_s, int rsub,
-                                         bool mirror, int ch) {
+// k (of K), of rows rsub, rsub + 16, ... of the tile: zero where the tap's
+// `need` mask meets the row's edge mask or k is past the end
+template <int VEC>
+__device__ __forceinline__ void gather01(float4 (&xv)[TB_M / 16], const float *__restrict__ A,
+                                         int k, int K, const TapEnt *taps, const int2 *rows_s,
+                                         int rsub, int ch) {
 #pragma unroll
   for (int it = 0; it < TB_M / 16; ++it) xv[it] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (VEC) {
-    if (k >= p.K) return;
+    if (k >= K) return;
     const int tap = k / ch, c = k - tap * ch;
-    if (MODE == 0 || mirror) {
-      const TapEnt t = taps[tap];
+    const TapEnt t = taps[tap];
 #pragma unroll
-      for (int it = 0; it < TB_M / 16; ++it) {
-        const int2 ri = rows_s[it * 16 + rsub];
-        if (!(ri.y & t.need))
-          xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)(ri.x + t.off) * ch + c));
-      }
-    } else {  // MODE 1, stride 2
-      int o[4];
-      tap_digits(tap, o);
-#pragma unroll
-      for (int it = 0; it < TB_M / 16; ++it) {
-        const int2 ri = rows_s[it * 16 + rsub];
-        bool ok = ri.y != 0;
-        int lin = 0, mul = 1;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const int num = ((ri.x >> (8 * a)) & 255) + 1 - o[a];
-          const int q = num >> 1;
-          ok = ok && num >= 0 && (num & 1) == 0 && q < p.rout;
-          lin += q * mul;
-          mul *= p.rout;
-        }
-        if (ok) xv[it] = __ldg(reinterpret_cast<const float4 *>(p.A + (size_t)lin * ch + c));
-      }
+    for (int it = 0; it < TB_M / 16; ++it) {
+      const int2 ri = rows_s[it * 16 + rsub];
+      if (!(ri.y & t.need))
+        xv[it] = __ldg(reinterpret_cast<const float4 *>(A + (size_t)(ri.x + t.off) * ch + c));
     }
-  } else {  // MODE 0 with a channel count that is not a multiple of 8
+  } else {  // a channel count that is not a multiple of 8 (the forward pass only)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int kj = k + j;
-      if (kj < p.K) {
-        const int tap = kj / p.cin, ci = kj - tap * p.cin;
+      if (kj < K) {
+        const int tap = kj / ch, ci = kj - tap * ch;
         const TapEnt t = taps[tap];
 #pragma unroll
         for (int it = 0; it < TB_M / 16; ++it) {
           const int2 ri = rows_s[it * 16 + rsub];
           if (!(ri.y & t.need)) {
-            const float v = __ldg(p.A + (size_t)(ri.x + t.off) * p.cin + ci);
+            const float v = __ldg(A + (size_t)(ri.x + t.off) * ch + ci);
             if (j == 0) xv[it].x = v;
             if (j == 1) xv[it].y = v;
             if (j == 2) xv[it].z = v;
@@ -188,7 +168,8 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t bars[2];
   __shared__ uint32_t tbase;
-  __shared__ TapEnt taps[81];     // MODE 0, and MODE 1 at stride 1
+  __shared__ TapEnt taps[81];     // MODE 0/1: the taps of the reduction
+  __shared__ int ctap[16];        // MODE 1 at stride 2: the class's tap numbers
   __shared__ int2 rows_s[TB_M];   // MODE 0/1: row table (see below)
   __shared__ int2 vtab[3][TB_K];  // MODE 2: voxel tables of three chunks
 
@@ -199,21 +180,53 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   const int N = p.N;
   const int nb = MODE == 2 ? 2 : 1;  // B tiles per stage
   const int stage_bytes = 2 * A_TILE + nb * N * TB_K * 2;
-  const int kbeg = blockIdx.z * p.kslice;
-  const int kend = min(p.K, kbeg + p.kslice);
-  const int kpad_end = MODE == 0 ? min(p.Kpad, kbeg + p.kslice) : kend;
-  const int nch = (kpad_end - kbeg + TB_K - 1) / TB_K;
   const int rin = p.rin, rout = p.rout;
   // MODE 1 at stride 1 reads the output gradient like a forward pass with
-  // mirrored taps; at stride 2 it decodes each row's coordinates
-  const bool mirror = MODE == 1 && p.stride == 1;
+  // mirrored taps.  At stride 2 an input voxel u = 2 w + par (per axis)
+  // receives only the taps o with u + 1 - o even: o = 1 where par_a = 0, o
+  // in {0, 2} where par_a = 1.  Block row blockIdx.y is the parity class par;
+  // its rows are the voxels w of the output-gradient grid and its reduction
+  // runs over its 1 to 16 taps, each reading w + (par + 1 - o) / 2.
+  const bool cls = MODE == 1 && p.stride == 2;
+  const int par = cls ? (int)blockIdx.y : 0;
+  int ntap_c = 0;
+  if (cls) {
+    ntap_c = 1;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) ntap_c *= 1 + ((par >> a) & 1);
+  }
+  const int Kc = cls ? ntap_c * p.cout : p.K;  // this block's reduction length
+  const int kbeg = blockIdx.z * p.kslice;
+  const int kend = min(Kc, kbeg + p.kslice);
+  const int kpad_end = MODE == 0 ? min(p.Kpad, kbeg + p.kslice) : kend;
+  const int nch = (kpad_end - kbeg + TB_K - 1) / TB_K;
 
   if (warp == 0) tmem_alloc(&tbase, (uint32_t)p.ncols);
   if (tid == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);
   }
-  if ((MODE == 0 || mirror) && tid < 81) {
+  if (cls && tid < ntap_c) {
+    // class tap tid: bit b of tid picks o = 0 or 2 on the b-th odd axis;
+    // `need` marks the axes read at w + 1 (invalid where w + 1 = rout)
+    int o[4], bit = 0, need = 0x100, off = 0, st = 1;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      if ((par >> a) & 1) {
+        o[a] = ((tid >> bit) & 1) ? 2 : 0;
+        ++bit;
+      } else {
+        o[a] = 1;
+      }
+      const int delta = (((par >> a) & 1) + 1 - o[a]) / 2;  // 0 or 1
+      need |= delta << a;
+      off += delta * st;
+      st *= rout;
+    }
+    taps[tid] = TapEnt{need, off};
+    ctap[tid] = o[0] + 3 * (o[1] + 3 * (o[2] + 3 * o[3]));
+  }
+  if ((MODE == 0 || (MODE == 1 && !cls)) && tid < 81) {
     // grid the taps read: the input (MODE 0) or the output gradient (MODE 1)
     const int e = MODE == 0 ? rin : rout;
     int o[4];
@@ -230,13 +243,13 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     taps[tid] = TapEnt{need, off};
   }
   // row table: MODE 0: (input voxel of row * stride, edge mask);
-  // MODE 1 mirrored: (row's voxel, edge mask in the output-gradient grid);
-  // MODE 1 at stride 2: (packed coordinates, valid)
+  // MODE 1 at stride 1: (row's voxel, edge mask in the output-gradient grid);
+  // MODE 1 at stride 2: (row's voxel w, bit a where w_a + 1 = rout)
   if ((MODE == 0 || MODE == 1) && tid < TB_M) {
     const int row = m0 + tid;
-    int2 e = make_int2(0, MODE == 1 && !mirror ? 0 : 0x100);
+    int2 e = make_int2(0, 0x100);
     if (row < p.M) {
-      const int ext = MODE == 0 ? rout : rin;
+      const int ext = MODE == 0 || cls ? rout : rin;
       int c[4], v = row;
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
@@ -248,10 +261,13 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
 #pragma unroll
         for (int a = 0; a < 4; ++a) s[a] = c[a] * p.stride;
         e = make_int2(s[0] + rin * (s[1] + rin * (s[2] + rin * s[3])), edge_mask(s, rin));
-      } else if (mirror) {
+      } else if (!cls) {
         e = make_int2(row, edge_mask(c, rout));
       } else {
-        e = make_int2(c[0] | (c[1] << 8) | (c[2] << 16) | (c[3] << 24), 1);
+        int m = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) m |= (c[a] + 1 >= rout) << a;
+        e = make_int2(row, m);
       }
     }
     rows_s[tid] = e;
@@ -303,7 +319,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   if (MODE == 2)
     gather2(xw, vtab[0], kgbase, need_t, src_t, off_t, xmask_t);
   else
-    gather01<MODE, VEC>(xv, p, kbeg + kgl * 8 + half * 4, taps, rows_s, rsub, mirror, ch);
+    gather01<VEC>(xv, p.A, kbeg + kgl * 8 + half * 4, Kc, taps, rows_s, rsub, ch);
 
   int issued = 0;  // chunks whose MMAs were issued (block-uniform)
   bool bad = false;
@@ -358,8 +374,9 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
           uint4 w = make_uint4(0, 0, 0, 0);
           if (MODE == 0) {
             w = __ldg(reinterpret_cast<const uint4 *>(p.Bw + (size_t)n * p.Kpad + k));
-          } else if (k < p.K) {
-            const int tap = k / p.cout, c0 = k - tap * p.cout;
+          } else if (k < Kc) {
+            const int t = k / p.cout, c0 = k - t * p.cout;
+            const int tap = cls ? ctap[t] : t;
             w = __ldg(reinterpret_cast<const uint4 *>(
                 p.Bw + ((size_t)tap * p.cin + n) * p.cout + c0));
           }
@@ -371,8 +388,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
         if (MODE == 2)
           gather2(xw, vtab[(i + 1) % 3], kgbase, need_t, src_t, off_t, xmask_t);
         else
-          gather01<MODE, VEC>(xv, p, k0 + TB_K + kgl * 8 + half * 4, taps, rows_s, rsub,
-                              mirror, ch);
+          gather01<VEC>(xv, p.A, k0 + TB_K + kgl * 8 + half * 4, Kc, taps, rows_s, rsub, ch);
       }
       fence_proxy_async_smem();
     }
@@ -411,6 +427,19 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     const int r = m0 + 32 * q4 + (tid & 31);
     const bool split = MODE == 2 || gridDim.z > 1;
     float *C = p.C + (split ? (size_t)blockIdx.z * p.M * N : 0);
+    // output row: the row itself, or for a parity class the input voxel
+    // u = 2 w + par of the row's voxel w
+    size_t orow = (size_t)r;
+    if (cls && r < p.M) {
+      int v = r, u = 0, mul = 1;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        u += (2 * (v % rout) + ((par >> a) & 1)) * mul;
+        v /= rout;
+        mul *= rin;
+      }
+      orow = (size_t)u;
+    }
     for (int c0 = 16 * (warp >> 2); c0 < N; c0 += 32) {
       float v[16];
       tmem_ld16(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0, v);
@@ -422,7 +451,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
             v[j] = p.relu && y < 0.f ? 0.f : y;
           }
         }
-        float4 *dst = reinterpret_cast<float4 *>(C + (size_t)r * N + c0);
+        float4 *dst = reinterpret_cast<float4 *>(C + orow * N + c0);
 #pragma unroll
         for (int q = 0; q < 4; ++q)
           dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
@@ -597,11 +626,11 @@ TcPlan tc_plan_for(long long M, long long K, int N) {
 }
 
 template <int MODE, int VEC>
-void launch_tc(const TcArgs &a0, int nz, cudaStream_t s) {
+void launch_tc(const TcArgs &a0, int nz, cudaStream_t s, int gy = 1) {
   TcArgs a = a0;
   a.ncols = pow2_cols(a.N);
   tc_attr<MODE, VEC>();
-  dim3 grid((a.M + TB_M - 1) / TB_M, 1, nz);
+  dim3 grid((a.M + TB_M - 1) / TB_M, gy, nz);
   k_conv_tc<MODE, VEC><<<grid, TB_T, tc_smem<MODE>(a.N), s>>>(a);
   // a refused launch (configuration) is reported here, not by a later sync
   fh::cuda_check(cudaGetLastError(), "k_conv_tc launch");
@@ -638,7 +667,7 @@ size_t net_tc_work(int rin, int rout, int cin, int cout, int ks) {
     const TcPlan pl = plan_fwd(Vo, net_tc_kpad(cin, ks), cin, cout);
     if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vo * cout);
   }
-  if (net_tc_bwd_data_ok(cin, cout, ks)) {
+  if (net_tc_bwd_data_ok(cin, cout, ks) && rin == rout) {  // stride 2 needs no slices
     const TcPlan pl = tc_plan_for<1, 1>(Vi, 81LL * cout, cin);
     if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vi * cin);
   }
@@ -702,8 +731,18 @@ void net_tc_conv_bwd_data(const float *dout, const uint16_t *wb, float *din, flo
   a.Bw = wb;
   a.err = err;
   a.rin = rin, a.rout = rout, a.cin = cin, a.cout = cout, a.stride = stride;
-  a.M = rin * rin * rin * rin;
   a.N = cin;
+  if (stride == 2) {
+    // 16 parity classes of rout^4 rows each, at most 16 taps: one slice
+    a.M = rout * rout * rout * rout;
+    a.K = 16 * cout;
+    a.Kpad = a.K;
+    a.kslice = (a.K + TB_K - 1) / TB_K * TB_K;
+    a.C = din;
+    launch_tc<1, 1>(a, 1, s, 16);
+    return;
+  }
+  a.M = rin * rin * rin * rin;
   a.K = 81 * cout;
   a.Kpad = a.K;
   const TcPlan pl = tc_plan_for<1, 1>(a.M, a.K, a.N);
