@@ -418,15 +418,22 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     if (!mbar_wait_bounded(&bars[last & 1], (last >> 1) & 1)) ok = false;
   }
   if (!ok) atomicExch(p.err, FLOF_DEV_ERR_TC_TIMEOUT);
-  ok = __syncthreads_and(ok) && issued > 0;
+  ok = __syncthreads_and(ok);
+  // a slice past this block's reduction (a parity class with fewer taps)
+  // contributes zeros
+  const bool empty = ok && issued == 0;
+  ok = ok && issued > 0;
   fence_after_sync();
-  if (ok) {
+  if (ok || empty) {
     // warp w reads tensor-memory lanes 32 (w % 4) .. + 31; warps 0-3 and
     // 4-7 take alternate 16-column groups
     const int q4 = warp & 3;
     const int r = m0 + 32 * q4 + (tid & 31);
     const bool split = MODE == 2 || gridDim.z > 1;
-    float *C = p.C + (split ? (size_t)blockIdx.z * p.M * N : 0);
+    // a slice holds every output row: M of them, or all rin^4 input voxels
+    // of the parity classes
+    const size_t rows_out = cls ? (size_t)rin * rin * rin * rin : (size_t)p.M;
+    float *C = p.C + (split ? (size_t)blockIdx.z * rows_out * N : 0);
     // output row: the row itself, or for a parity class the input voxel
     // u = 2 w + par of the row's voxel w
     size_t orow = (size_t)r;
@@ -442,7 +449,12 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     }
     for (int c0 = 16 * (warp >> 2); c0 < N; c0 += 32) {
       float v[16];
-      tmem_ld16(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0, v);
+      if (ok) {
+        tmem_ld16(tacc + ((uint32_t)(32 * q4) << 16) + (uint32_t)c0, v);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.f;
+      }
       if (r < p.M) {
         if (!split && MODE == 0) {
 #pragma unroll
@@ -636,6 +648,18 @@ void launch_tc(const TcArgs &a0, int nz, cudaStream_t s, int gy = 1) {
   fh::cuda_check(cudaGetLastError(), "k_conv_tc launch");
 }
 
+// Slices of a stride-2 input gradient (16 parity classes of M rows, at most K
+// = 16 cout reduction entries): enough blocks for about three per SM, at
+// least two chunks per slice.
+int cls_slices(long long M, long long K) {
+  const long long blocks = (M + TB_M - 1) / TB_M * 16;
+  const long long chunks = (K + TB_K - 1) / TB_K;
+  long long nz = (3LL * sm_count() + blocks - 1) / blocks;
+  nz = std::min(nz, std::max(chunks / 2, 1LL));
+  const long long per = (chunks + nz - 1) / nz;
+  return (int)((chunks + per - 1) / per);
+}
+
 TcPlan plan_fwd(long long M, long long K, int cin, int cout) {
   return cin % 8 == 0 ? tc_plan_for<0, 1>(M, K, cout) : tc_plan_for<0, 0>(M, K, cout);
 }
@@ -667,9 +691,10 @@ size_t net_tc_work(int rin, int rout, int cin, int cout, int ks) {
     const TcPlan pl = plan_fwd(Vo, net_tc_kpad(cin, ks), cin, cout);
     if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vo * cout);
   }
-  if (net_tc_bwd_data_ok(cin, cout, ks) && rin == rout) {  // stride 2 needs no slices
-    const TcPlan pl = tc_plan_for<1, 1>(Vi, 81LL * cout, cin);
-    if (pl.nz > 1) w = std::max(w, (size_t)pl.nz * (size_t)Vi * cin);
+  if (net_tc_bwd_data_ok(cin, cout, ks)) {
+    const int nz = rin == rout ? tc_plan_for<1, 1>(Vi, 81LL * cout, cin).nz
+                               : cls_slices(Vo, 16LL * cout);
+    if (nz > 1) w = std::max(w, (size_t)nz * (size_t)Vi * cin);
   }
   if (net_tc_bwd_weight_ok(cin, cout, ks)) {
     const TcPlan pl = tc_plan_for<2, 0>(81LL * cin + 1, Vo, cout);
@@ -733,13 +758,19 @@ void net_tc_conv_bwd_data(const float *dout, const uint16_t *wb, float *din, flo
   a.rin = rin, a.rout = rout, a.cin = cin, a.cout = cout, a.stride = stride;
   a.N = cin;
   if (stride == 2) {
-    // 16 parity classes of rout^4 rows each, at most 16 taps: one slice
+    // 16 parity classes of rout^4 rows each, at most 16 taps
     a.M = rout * rout * rout * rout;
     a.K = 16 * cout;
     a.Kpad = a.K;
-    a.kslice = (a.K + TB_K - 1) / TB_K * TB_K;
-    a.C = din;
-    launch_tc<1, 1>(a, 1, s, 16);
+    const int nz = cls_slices(a.M, a.K);
+    const int chunks = (a.K + TB_K - 1) / TB_K;
+    a.kslice = (chunks + nz - 1) / nz * TB_K;
+    a.C = nz > 1 ? work : din;
+    launch_tc<1, 1>(a, nz, s, 16);
+    if (nz > 1) {
+      const long long n = (long long)rin * rin * rin * rin * cin;
+      k_sum_slices_epi<<<grid_for(n, 256), 256, 0, s>>>(work, din, n, nz, cin, nullptr, 0);
+    }
     return;
   }
   a.M = rin * rin * rin * rin;
