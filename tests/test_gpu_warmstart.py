@@ -61,13 +61,14 @@ def test_gradients_match_finite_differences(gpu):
     assert np.abs(gg - fd).max() <= 2e-3 * scale + 1e-7, np.c_[gg, fd]
 
 
-def test_full_gradient_at_16_matches_oracle(gpu):
+@pytest.mark.parametrize("R", [16, 12])
+def test_full_gradient_matches_oracle(gpu, R):
     """At the coarse extent the driver uses (16^4) every tensor-core shape
     runs: unsplit tiles with the bias and ReLU epilogue, split reductions, the
-    two-channel first layer, stride-2 input gradients.  The forward pass and
-    the whole gradient (every weight and bias) are compared with the oracle's
-    analytic backward pass (itself checked against finite differences)."""
-    R = 16
+    two-channel first layer, stride-2 input gradients by parity class.  12^4
+    has levels 12, 6 and 3 (no power of two).  The forward pass and the whole
+    gradient (every weight and bias) are compared with the oracle's analytic
+    backward pass (itself checked against finite differences)."""
     m = F.Model(R, seed=8)
     p = W.bf16_round(m.get_params())
     m.set_params(p)
