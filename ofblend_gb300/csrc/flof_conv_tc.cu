@@ -42,8 +42,8 @@ using namespace tc;
 
 constexpr int TB_M = 128;  // rows per block (the MMA's M)
 constexpr int TB_K = 64;   // reduction entries per chunk (four K = 16 MMAs)
-constexpr int TB_T = 256;  // threads: two per row, each staging half the reduction groups
-constexpr int KG_T = 8 * TB_M / TB_T;  // reduction groups (of 8) per thread and chunk
+constexpr int TB_T = 256;  // threads
+constexpr int KG_T = 8 * TB_M / TB_T;  // weight gradient: reduction groups (of 8) per thread
 constexpr int A_TILE = TB_M * TB_K * 2;  // bytes of one BF16 A tile
 
 struct TcArgs {
@@ -59,10 +59,12 @@ struct TcArgs {
   int bias_row;           // MODE 2: the last row is all ones (the bias gradient)
 };
 
-// (tap, channel) reduction entries of a 3^4 tap with offsets o in 0..2 per
-// axis: `need` has bit a set when o_a = 0 and bit 4 + a when o_a = 2, plus
-// bit 8 (never valid for an invalid row or voxel); `off` is the tap's
-// linear voxel offset sum (o_a - 1) stride_a in the grid it reads.
+// A tap of the reduction: its source voxel is the row's voxel plus `off`
+// (linear, in the grid the tap reads), and it falls off that grid for rows
+// whose edge mask shares a bit with `need`.  For a forward tap with offsets
+// o in 0..2 per axis, `need` has bit a where o_a = 0 and bit 4 + a where
+// o_a = 2, and off = sum (o_a - 1) stride_a.  Bit 8 is always set, so an
+// invalid row (edge mask 0x100) reads nothing.
 struct TapEnt {
   int need, off;
 };
