@@ -52,10 +52,13 @@ def args_():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-pairs", type=int, default=256)
     ap.add_argument("--train-epochs", type=int, default=20)
-    ap.add_argument("--workload", default="flof", choices=["flof", "batch", "mixed", "learned"],
+    ap.add_argument("--workload", default="flof",
+                    choices=["flof", "batch", "mixed", "learned", "net"],
                     help="flof: the two-way 64^4 workload (default); batch: 64 independent solves of "
                          "uneven sizes, concurrent against sequential; mixed: the 96^4 solve in mixed "
-                         "precision against FP32")
+                         "precision against FP32; learned: train the warm start and solve with it; "
+                         "net: the network's training step alone")
+    ap.add_argument("--net-batch", type=int, default=16)
     ap.add_argument("--batch-pairs", type=int, default=64)
     ap.add_argument("--batch-workers", type=int, default=0)
     return ap.parse_args()
@@ -731,6 +734,48 @@ def run_learned(a):
     ctx.close()
 
 
+def run_net(a):
+    """The warm-start network's training step alone: Adam steps of a batch of
+    --net-batch seeded random samples at the coarse extent 16^4 (the
+    tcgen05 convolutions, their gradients and the update)."""
+    import numpy as np
+    import torch
+    import ofblend_gb300 as F
+    torch.cuda.set_device(0)
+    ctx = F.Context(0)
+    R = 16
+    m = F.Model(R, ctx=ctx, seed=1)
+    rng = np.random.default_rng(0)
+    d = (R,) * 4
+    samples = [(F.Grid4Real(dims=d, ctx=ctx).from_numpy((rng.standard_normal(d) * 0.004).astype(np.float32)),
+                F.Grid4Real(dims=d, ctx=ctx).from_numpy((rng.standard_normal(d) * 0.004).astype(np.float32)),
+                F.Grid4Vec4(dims=d, ctx=ctx).from_numpy((rng.standard_normal(d + (4,)) * 0.5).astype(np.float32)))
+               for _ in range(max(a.net_batch, 1))]
+    for _ in range(a.warmup):
+        m.train_step(samples, 1e-3)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        m.train_step(samples, 1e-3)  # returns after the step has finished
+    sec = (time.perf_counter() - t0) / max(a.steps, 1)
+    sps = len(samples) / sec
+    ach = net_train_flops(R) * sps / 1e12
+    pk, pk_kind = measured_bf16_tflops()
+    print(json.dumps({
+        "metric": "warm-start network training samples/s at 16^4", "value": round(sps, 2),
+        "unit": "samples/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": round(sec * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "bf16 tcgen05 MMAs (activations and gradients as bf16 hi/lo pairs), f32 accumulation",
+        "data": "synthetic (seeded normal inputs and targets)",
+        "config": {"workload": f"Adam steps of {len(samples)} samples at 16^4", "batch": len(samples)},
+        "roofline": {"bound": "tensor", "region": "whole training step", "achieved": round(ach, 3),
+                     "peak": pk, "unit": "TFLOP/s", "frac": round(ach / pk, 5), "traffic": None,
+                     "peak_source": f"bf16_tflops of {pk_kind}"}}), flush=True)
+    m.free()
+    ctx.close()
+
+
 if __name__ == "__main__":
     a = args_()
     if a.impl == "reference":
@@ -741,5 +786,7 @@ if __name__ == "__main__":
         run_mixed(a)
     elif a.workload == "learned":
         run_learned(a)
+    elif a.workload == "net":
+        run_net(a)
     else:
         run_gpu(a)
