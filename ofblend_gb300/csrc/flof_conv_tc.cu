@@ -13,8 +13,8 @@
 // Per block: 256 threads gather a 128 x 64 reduction chunk of the operand
 // (im2col on the fly: voxel rows x (tap, channel), or (tap, channel) rows x
 // voxels for the weight gradient) through registers into shared memory in
-// the 128-byte-swizzled K-major layout (flof_tcgen05.cuh), while thread 0's
-// MMAs of the previous chunk run; two stages, each released by a
+// the 128-byte-swizzled K-major layout (flof_tcgen05.cuh), while the
+// previous chunk's MMAs (issued by a ninth warp) run; two stages, each released by a
 // tcgen05.commit on its mbarrier.  The forward and input-gradient gathers
 // run along channels (16 lanes read 256 contiguous bytes of a row), the
 // weight-gradient gather along the (tap, channel) rows.  The weight
@@ -42,7 +42,8 @@ using namespace tc;
 
 constexpr int TB_M = 128;  // rows per block (the MMA's M)
 constexpr int TB_K = 64;   // reduction entries per chunk (four K = 16 MMAs)
-constexpr int TB_T = 256;  // threads
+constexpr int TB_T = 256;  // threads that stage operands
+constexpr int TB_W = TB_T + 32;  // plus one warp that issues the MMAs
 constexpr int KG_T = 8 * TB_M / TB_T;  // weight gradient: reduction groups (of 8) per thread
 constexpr int A_TILE = TB_M * TB_K * 2;  // bytes of one BF16 A tile
 
@@ -166,7 +167,7 @@ __device__ __forceinline__ void gather2(float (&xw)[KG_T][8], const int2 *vt, in
 }
 
 template <int MODE, int VEC>
-__global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
+__global__ void __launch_bounds__(TB_W, 3) k_conv_tc(TcArgs p) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ uint64_t bars[2];
   __shared__ uint32_t tbase;
@@ -318,10 +319,15 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   // MMA issue and the next stage's wait.
   float4 xv[TB_M / 16];  // MODE 0/1
   float xw[KG_T][8];     // MODE 2
-  if (MODE == 2)
-    gather2(xw, vtab[0], kgbase, need_t, src_t, off_t, xmask_t);
-  else
-    gather01<VEC>(xv, p.A, kbeg + kgl * 8 + half * 4, Kc, taps, rows_s, rsub, ch);
+  // warps 0-7 stage the operands; warp 8 only issues the MMAs, so that the
+  // staging warps do not wait at the next barrier for the issuing thread
+  const bool producer = tid < TB_T;
+  if (producer) {
+    if (MODE == 2)
+      gather2(xw, vtab[0], kgbase, need_t, src_t, off_t, xmask_t);
+    else
+      gather01<VEC>(xv, p.A, kbeg + kgl * 8 + half * 4, Kc, taps, rows_s, rsub, ch);
+  }
 
   int issued = 0;  // chunks whose MMAs were issued (block-uniform)
   bool bad = false;
@@ -331,8 +337,8 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
     unsigned char *st = smem + s * stage_bytes;
     unsigned char *Ahi = st, *Alo = st + A_TILE, *Bhi = st + 2 * A_TILE;
     unsigned char *Blo = Bhi + N * TB_K * 2;
-    if (i >= 2 && !mbar_wait_bounded(&bars[s], ((i - 2) >> 1) & 1)) bad = true;
-    if (!bad) {
+    if (producer && i >= 2 && !mbar_wait_bounded(&bars[s], ((i - 2) >> 1) & 1)) bad = true;
+    if (producer && !bad) {
       if (MODE == 2)
         fill_vtab(vtab[(i + 2) % 3], tid, kbeg, i + 2, nch, kend, rout, rin, p.stride, p.cin);
       // ---- A: store this chunk's registers
@@ -395,7 +401,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
       fence_proxy_async_smem();
     }
     if (__syncthreads_or(bad)) break;
-    if (tid == 0) {
+    if (tid == TB_T) {
       fence_after_sync();
       const uint32_t a_hi = smem_addr(Ahi), a_lo = smem_addr(Alo);
       const uint32_t b_hi = smem_addr(Bhi), b_lo = smem_addr(Blo);
@@ -426,7 +432,7 @@ __global__ void __launch_bounds__(TB_T, 3) k_conv_tc(TcArgs p) {
   const bool empty = ok && issued == 0;
   ok = ok && issued > 0;
   fence_after_sync();
-  if (ok || empty) {
+  if ((ok || empty) && producer) {
     // warp w reads tensor-memory lanes 32 (w % 4) .. + 31; warps 0-3 and
     // 4-7 take alternate 16-column groups
     const int q4 = warp & 3;
@@ -626,7 +632,7 @@ int tc_resident(int N) {
   if (known > 0) return known;
   tc_attr<MODE, VEC>();
   int nb = 0;
-  fh::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<MODE, VEC>, TB_T,
+  fh::cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_conv_tc<MODE, VEC>, TB_W,
                                                                tc_smem<MODE>(N)),
                  "cudaOccupancyMaxActiveBlocksPerMultiprocessor(k_conv_tc)");
   nb = std::max(nb, 1);
@@ -645,7 +651,7 @@ void launch_tc(const TcArgs &a0, int nz, cudaStream_t s, int gy = 1) {
   a.ncols = pow2_cols(a.N);
   tc_attr<MODE, VEC>();
   dim3 grid((a.M + TB_M - 1) / TB_M, gy, nz);
-  k_conv_tc<MODE, VEC><<<grid, TB_T, tc_smem<MODE>(a.N), s>>>(a);
+  k_conv_tc<MODE, VEC><<<grid, TB_W, tc_smem<MODE>(a.N), s>>>(a);
   // a refused launch (configuration) is reported here, not by a later sync
   fh::cuda_check(cudaGetLastError(), "k_conv_tc launch");
 }
