@@ -156,6 +156,16 @@ def measured_bf16_tflops():
     return 1900.0, "fallback"
 
 
+def step_hbm(recs, steps, ms, peak, peak_kind):
+    """HBM rate of the whole step on one GPU: the algorithmic bytes of every
+    launch (each kernel class's per-cell bytes; kernels bound by arithmetic
+    count their compulsory bytes only) over the untraced step time."""
+    b = sum(r[2] for r in recs) / steps
+    gbs = b / (ms / steps * 1e-3) / 1e9
+    return {"bytes_per_step": round(b), "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(gbs / peak, 4), "peak_source": f"hbm_gbs of {peak_kind}"}
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes (read + write) of the kernel classes measured by
     ncu at 64^4, from the committed summary's table (profiles/)."""
@@ -471,6 +481,7 @@ def run_gpu(a):
         "gpu_launches": launches,
         "clocks": clk,
         "kernel_share": share,
+        "hbm_step": step_hbm(recs, a.steps, ms_max, peak, peak_kind),
         "kernel_ms_per_step": round(sum(r[3] for r in recs) / a.steps, 3),
         "ms_per_step_profiled": round(ms_prof / a.steps, 3),
         "cg_iterations_level0": [[x[1] for x in s if x[0] == a.res] for s in iters[:2]],
