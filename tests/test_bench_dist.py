@@ -85,3 +85,21 @@ def test_reference_arm_reports_from_rank_zero_only(monkeypatch, capsys):
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"] == bench.flof_config(_args(), 2)
     assert line["metric"] == bench.METRIC and line["higher_is_better"] is True
+
+
+def test_step_hbm_and_network_flops():
+    sys.path.insert(0, ROOT)
+    import bench
+    recs = [("cg_matvec", 64, 1.0e9, 0.2), ("gauss_blur", 64, 2.0e9, 1.0)]
+    h = bench.step_hbm(recs, 2, 100.0, 6800.0, "measured")
+    assert h["bytes_per_step"] == 1.5e9
+    assert h["achieved"] == pytest.approx(1.5e9 / 0.05 / 1e9, rel=1e-3)
+    assert h["frac"] == pytest.approx(h["achieved"] / 6800.0, abs=1e-4)  # rounded to 4 places
+    # 2 * taps * cin * cout per output voxel and layer; training = forward,
+    # weight gradients and the input gradients of every layer but the first
+    R = 16
+    fwd = (2 * 81 * (2 * 16 * R ** 4 + 16 * 32 * (R // 2) ** 4 + 32 * 32 * (R // 2) ** 4
+                     + 32 * 64 * (R // 4) ** 4 + 64 * 64 * (R // 4) ** 4 + 96 * 32 * (R // 2) ** 4
+                     + 48 * 16 * R ** 4) + 2 * 16 * 4 * R ** 4)
+    assert bench.net_flops(R) == fwd
+    assert bench.net_train_flops(R) == 3 * fwd - 2 * 81 * 2 * 16 * R ** 4
