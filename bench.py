@@ -48,7 +48,7 @@ def args_():
     ap.add_argument("--hires", type=int, default=128)
     ap.add_argument("--cg-accuracy", type=float, default=1e-4)
     ap.add_argument("--blur-type", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-pairs", type=int, default=256)
     ap.add_argument("--train-epochs", type=int, default=20)
