@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "4D flow solves/s at 64^4 to fixed residual: learned warm-start vs plain CG"
+NFRAMEBUF = 4  # device frame buffers of the e2e pipeline
 UNIT = "solves/s"
 ALPHAS = (0.25, 0.5, 0.75)
 
@@ -209,7 +210,8 @@ class Workload:
         self.v01, self.v10 = mk(F.Grid4Vec4, dims), mk(F.Grid4Vec4, dims)
         self.out4 = mk(F.Grid4Real, dims)
         self.dst = mk(F.RealGrid, (H, H, H, 1))
-        self.dst2 = mk(F.RealGrid, (H, H, H, 1))  # second frame buffer of the e2e pipeline
+        # further frame buffers of the e2e pipeline (downloads in flight)
+        self.dsts = [self.dst] + [mk(F.RealGrid, (H, H, H, 1)) for _ in range(NFRAMEBUF - 1)]
         self.factor = (H / R, H / R, H / R, self.Tf / R)
         self.bord = int(H * 0.1)
         self.stats = []
@@ -248,8 +250,8 @@ class Workload:
         """One step through the C ABI from and to host buffers, with the
         transfers pipelined on the context's copy stream: the solves wait only
         for their own inputs (the mode-2 and hi-res inputs upload meanwhile),
-        results download while later work runs, and frames alternate between
-        two device buffers.  Ends when every result is in host memory."""
+        results download while later work runs, and frames rotate through
+        NFRAMEBUF device buffers.  Ends when every result is in host memory."""
         F = self.F
         for n in ("i0", "i1", "s0", "s1", "hi0", "hi1"):
             getattr(self, "g_" + n).upload_async(pinned[n])
@@ -277,13 +279,13 @@ class Workload:
         n = 0
         for a in ALPHAS:
             for t in range(Tf):
-                d = (self.dst, self.dst2)[n % 2]
+                d = self.dsts[n % NFRAMEBUF]
                 d.copy_wait()
                 F.loadAdvectTimeSlice_OptRunTwoway(1, 2, d, self.g_hi0, self.g_hi1, t + 0.5, a, 1.0,
                                                    (0, 0, 0, 0), (1, 1, 1, Tf / Tf), self.factor,
                                                    overrideSize=(H, H, H, Tf), overrideTimeOff=0.0,
                                                    bordSkip=self.bord)
-                d.download_async(sink["frame"][n % 2])
+                d.download_async(sink["frame"][n % NFRAMEBUF])
                 n += 1
         F.loadAdvectTimeSlice_Finish(1)
         F.loadAdvectTimeSlice_Finish(2)
@@ -455,7 +457,7 @@ def run_gpu(a):
     pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
     sink = {"v01": pin(W.v01.shape), "v10": pin(W.v10.shape),
             "out4": [pin(W.out4.shape) for _ in ALPHAS],
-            "frame": [pin(W.dst.shape), pin(W.dst.shape)]}
+            "frame": [pin(W.dst.shape) for _ in range(NFRAMEBUF)]}
     e2e_val = None
     if a.e2e_steps > 0:
         W.step_e2e(pinned, sink, ctx)
