@@ -153,8 +153,16 @@ FLOF_API const char *flof_kernel_class_name(int cls);
  * FLOF_OPT_AUTOTUNE: 1 times a few launch shapes of the PCG kernels once per
  *   grid size and keeps the fastest; 0 (default) uses fixed shapes.  Shapes
  *   group the dot-product partial sums differently, so tuned and untuned runs
- *   agree to rounding, not bit for bit. */
-enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3 };
+ *   agree to rounding, not bit for bit.
+ * FLOF_OPT_STRICT: 1 runs the FP32 PCG with the reference's arithmetic
+ *   operation for operation (GridCGOptflow4d::solve, optflow4d.cpp:268-329:
+ *   double alpha and beta, addScaled's double multiply and add rounded once
+ *   to float, dotProd's serial double sum in row order) and sums the error
+ *   metric serially in calcLsDiffTempl's loop order (:895-927), so that
+ *   whole solves equal the reference's bit for bit.  One thread forms each
+ *   sum: for parity checks on grids of a few million cells, not for speed.
+ *   0 (default): the parallel kernels. */
+enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3, FLOF_OPT_STRICT = 4 };
 FLOF_API int flof_ctx_set_option(flof_ctx *ctx, int option, int value);
 /* Release cached device buffers of the context's pool (and its workers'). */
 FLOF_API int flof_ctx_trim(flof_ctx *ctx);
@@ -266,7 +274,11 @@ FLOF_API int flof_gaussianBlur4d(flof_ctx *ctx, flof_grid *a, float sigma,
 FLOF_API int flof_advect4d(flof_ctx *ctx, const flof_grid *vel,
                            flof_grid *grid, float dtFac);
 
-/* calcLsDiff4d (optflow4d.cpp:2132-2137 -> calcLsDiffTempl :895-927). */
+/* calcLsDiff4d (optflow4d.cpp:2132-2137 -> calcLsDiffTempl :895-927).
+ * Every axis loses 2 bnd cells, T and Z included: Grid4d's is3D() and
+ * is4D() are constant true (grid4d.h:82-83).  A bnd that leaves no cells
+ * gives the reference's 0 * (1 / count): -0 for a negative count, NaN for
+ * a zero one.  bnd must be in [0, 2^20]. */
 FLOF_API int flof_calcLsDiff4d(flof_ctx *ctx, const flof_grid *i0,
                                const flof_grid *i1, flof_grid *out,
                                float correction, int bnd, float *result);
@@ -295,19 +307,22 @@ FLOF_API int flof_deform4d(flof_ctx *ctx, flof_grid *out, const flof_grid *i0,
 
 /* calcLsDiff4d without any device allocation.  This entry point has no
  * counterpart in the reference.  It is for callers that cannot allocate
- * device memory where they need the error metric: code recorded into a CUDA
- * graph by stream capture (allocation cannot be captured) and applications
- * that reserve all device memory at start-up.  It computes the same value
- * as flof_calcLsDiff4d (calcLsDiffTempl, optflow4d.cpp:895-927) from the
- * caller's device buffers on the caller's stream (void* cudaStream_t, NULL
- * for the legacy default stream) and writes it to the device float
- * `result`; `out` (device, nullable) receives the per-cell values.
+ * device memory where they need the error metric: applications that reserve
+ * all device memory at start-up and forbid allocations afterwards, and loops
+ * that cannot afford one (an allocation may synchronise the device).  It
+ * computes the same value as flof_calcLsDiff4d (calcLsDiffTempl,
+ * optflow4d.cpp:895-927) from the caller's device buffers on the caller's
+ * stream (void* cudaStream_t, NULL for the legacy default stream) and writes
+ * it to the device float `result`; `out` (device, nullable) receives the
+ * per-cell values.  A bnd that leaves no cells gives the reference's
+ * 0 * (1 / count) (-0 or NaN), as flof_calcLsDiff4d does.
  * Grids up to 2^31-1 cells; larger ones are rejected with FLOF_E_ARG.
  * Its scratch is a fixed 8 KiB device array in the library (1024 block
  * partials plus a counter), held by every GPU that loads the library until
  * exit and shared by all calls: calls that overlap on the GPU race on it.
- * The first call on a device looks the array's address up; make that first
- * call before any stream capture. */
+ * Outside stream capture every call looks the array's address up for the
+ * current context; a captured call uses the address of the last ordinary
+ * call on that device, so make an ordinary call first. */
 FLOF_API int flof_calcLsDiff4d_noalloc(const float *i0, const float *i1,
                                        float *out, const int dims[4],
                                        float correction, int bnd,

@@ -16,6 +16,7 @@ FLOF_REAL = 1
 FLOF_VEC4 = 8
 FLOF_OPT_CFL_SYNC = 2
 FLOF_OPT_AUTOTUNE = 3
+FLOF_OPT_STRICT = 4
 FLOF_PRECISION_FP32 = 0
 FLOF_PRECISION_MIXED = 1
 MAX_SOLVE_STATS = 64

@@ -93,9 +93,13 @@ void advect_cfl(flof_ctx *c, Dims4 d, float cfl, const float4 *vel, float *grid,
 // calcLsDiffTempl (optflow4d.cpp:895-927), synchronising.
 float ls_diff(flof_ctx *c, const float *i0, const float *i1, float *out, Dims4 d, float corr,
               int bnd) {
-  KLP(c, KC_LSDIFF, d.x, d.cells() * 8,
-      launch_ls_diff(i0, i1, out, d, corr, bnd, c->dpart, c->counter + 5, c->dres + 0,
-                       c->fres + 1, c->stream));
+  if (c->strict)
+    KLP(c, KC_LSDIFF, d.x, d.cells() * 8,
+        launch_strict_ls_diff(i0, i1, out, d, corr, bnd, c->dres + 0, c->fres + 1, c->stream));
+  else
+    KLP(c, KC_LSDIFF, d.x, d.cells() * 8,
+        launch_ls_diff(i0, i1, out, d, corr, bnd, c->dpart, c->counter + 5, c->dres + 0,
+                         c->fres + 1, c->stream));
   return read_f(c, c->fres + 1);
 }
 
@@ -327,6 +331,26 @@ void pcg_loop(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, float4 
   }
 }
 
+// The PCG with the reference's arithmetic (FLOF_OPT_STRICT): the same
+// chunked launches and host checks as pcg_loop, one strict iteration per
+// step.
+void pcg_loop_strict(flof_ctx *c, Dims4 d, const OFConsts &k, float4 *x, float4 *r, float4 *p,
+                     float4 *q, const float4 *g, int maxIter) {
+  KL(c, launch_strict_init(r, g, d, k, c->st, c->stream));
+  int it = 0;
+  for (;;) {
+    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (c->st_h->done != CG_RUNNING || it >= maxIter) break;
+    const int n = (maxIter - it) < 16 ? (maxIter - it) : 16;
+    for (int s = 0; s < n; ++s)
+      KLP(c, KC_MATVEC, d.x, nint(d) * 160,
+          launch_strict_iteration(x, r, p, q, g, d, k, c->st, c->dpart, c->fpart, maxIter,
+                                  c->stream));
+    it += n;
+  }
+}
+
 // Mixed-precision solve with iterative refinement.  The PCG runs on the
 // matrix of the BF16-stored gradient, first to sqrt(cgAccuracy) (restarting
 // from the assembly's r = b with that matrix's preconditioner).  Then, up to
@@ -414,7 +438,10 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
   if (a.precision != FLOF_PRECISION_MIXED) {
-    pcg_loop(c, d, k, tu, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter, i1);
+    if (c->strict)
+      pcg_loop_strict(c, d, k, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter);
+    else
+      pcg_loop(c, d, k, tu, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter, i1);
     int status = c->st_h->done;
     if (status == CG_RUNNING) status = CG_MAXITER;  // cgMaxIter == 0
     const int iters = c->st_h->iters;
@@ -876,6 +903,10 @@ FLOF_API int flof_ctx_set_option(flof_ctx *c, int option, int value) {
     if (option == FLOF_OPT_CFL_SYNC) {
       need(value == 0 || value == 1, "FLOF_OPT_CFL_SYNC takes 0 or 1");
       c->cfl_force_sync = value;
+    } else if (option == FLOF_OPT_STRICT) {
+      need(value == 0 || value == 1, "FLOF_OPT_STRICT takes 0 or 1");
+      c->strict = value;
+      for (flof_ctx *w : c->workers) w->strict = value;
     } else if (option == FLOF_OPT_AUTOTUNE) {
       need(value == 0 || value == 1, "FLOF_OPT_AUTOTUNE takes 0 or 1");
       c->autotune = value;
@@ -1363,9 +1394,8 @@ FLOF_API int flof_calcLsDiff4d(flof_ctx *c, const flof_grid *i0, const flof_grid
       need_elem(out, FLOF_REAL, "out");
       same_size(i0, out, "calcLsDiff4d");
     }
-    need(bnd >= 0 && 2 * bnd < i0->dims[0] && 2 * bnd < i0->dims[1] && 2 * bnd < i0->dims[2] &&
-             2 * bnd < i0->dims[3],
-         "calcLsDiff4d: bnd leaves no cells");
+    // a bnd that leaves no cells gives the reference's 0 * (1 / count)
+    need(bnd >= 0 && bnd <= (1 << 20), "calcLsDiff4d: bnd must be in [0, 2^20]");
     set_ctx_device(c);
     const float r = ls_diff(c, i0->f(), i1->f(), out ? out->f() : nullptr, i0->D(), correction,
                             bnd);

@@ -153,6 +153,8 @@ struct flof_ctx {
   // autotuned PCG launch shapes per grid size (FLOF_OPT_AUTOTUNE); worker
   // contexts share their parent's table (tune_owner)
   int autotune = 0;
+  // FLOF_OPT_STRICT: the reference's PCG and error-metric arithmetic
+  int strict = 0;
   std::map<std::array<int, 4>, flof::CGTune> tunes;
   std::mutex tune_mu;
   flof_ctx *tune_owner = nullptr;

@@ -158,6 +158,21 @@ void launch_cg_update(float4 *r, const float4 *q, const BF4 *g, Dims4 d, OFConst
 void launch_cg_direction(float4 *x, float4 *p, const float4 *r, const BF4 *g, Dims4 d,
                          OFConsts c, CGState *st, cudaStream_t s,
                          const CGTune &tu = CGTune());
+// ---- strict arithmetic (flof_strict.cu, FLOF_OPT_STRICT) ----------------------
+// The reference's PCG arithmetic operation for operation: double alpha and
+// beta, double multiply-and-add updates rounded once to float, and dot
+// products summed serially in the reference's row order by one thread.
+// launch_strict_init follows launch_of_assemble_init (it replaces the
+// parallel z.r with the serial one); one launch_strict_iteration is one PCG
+// iteration (matvec, p.q, x and r updates with the stop rule, z.r, new p).
+void launch_strict_init(const float4 *r, const float4 *g, Dims4 d, OFConsts c, CGState *st,
+                        cudaStream_t s);
+void launch_strict_iteration(float4 *x, float4 *r, float4 *p, float4 *q, const float4 *g, Dims4 d,
+                             OFConsts c, CGState *st, double *dpart, float *fpart, int maxIter,
+                             cudaStream_t s);
+// calcLsDiffTempl with the serial double sum in the reference's loop order.
+void launch_strict_ls_diff(const float *i0, const float *i1, float *out, Dims4 d, float correction,
+                           int bnd, double *result_d, float *result_f, cudaStream_t s);
 // ---- mixed precision (flof_mixed.cu) ------------------------------------------
 // g16 = bf16(g) over n cells
 void launch_to_bf4(const float4 *g, BF4 *g16, long long n, cudaStream_t s);

@@ -2,13 +2,13 @@
 // memory.
 //
 // Some callers of this library cannot call cudaMalloc at the point where they
-// need the level-set error metric.  Examples are code recorded into a CUDA
-// graph by stream capture, where an allocation is not a capturable operation,
-// and host applications that reserve all device memory at start-up and
-// forbid allocations afterwards.  flof_calcLsDiff4d needs a context, and a
-// context owns a device pool.  flof_calcLsDiff4d_noalloc takes the caller's
-// device buffers and keeps its only scratch, the per-block partial sums of
-// the reduction, in a file-scope device array instead.
+// need the level-set error metric.  Examples are host applications that
+// reserve all device memory at start-up and forbid allocations afterwards,
+// and loops that must not pay for an allocation, which may synchronise the
+// whole device.  flof_calcLsDiff4d needs a context, and a context owns a
+// device pool.  flof_calcLsDiff4d_noalloc takes the caller's device buffers
+// and keeps its only scratch, the per-block partial sums of the reduction,
+// in a file-scope device array instead.
 //
 // The array is part of the library image: every GPU that loads the library
 // holds it (8 KiB) until the process exits.  All calls share it and it keeps
@@ -95,19 +95,28 @@ extern "C" FLOF_API int flof_calcLsDiff4d_noalloc(const float *i0, const float *
   const long long cells = (long long)dims[0] * dims[1] * dims[2] * dims[3];
   if (cells >= (1ll << 31))
     return na_fail(FLOF_E_ARG, "grid too large for calcLsDiff4d_noalloc: at most 2^31-1 cells");
+  if (bnd < 0 || bnd > (1 << 20))
+    return na_fail(FLOF_E_ARG, "calcLsDiff4d_noalloc: bnd must be in [0, 2^20]");
   const int ex = dims[0] - 2 * bnd, ey = dims[1] - 2 * bnd, ez = dims[2] - 2 * bnd,
             et = dims[3] - 2 * bnd;
-  if (bnd < 0 || ex <= 0 || ey <= 0 || ez <= 0 || et <= 0)
-    return na_fail(FLOF_E_ARG, "calcLsDiff4d_noalloc: bnd leaves no cells");
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES)
     return na_fail(FLOF_E_CUDA, "calcLsDiff4d_noalloc: no usable current device");
+  cudaStream_t s = (cudaStream_t)stream;
+  // The array's device address belongs to the context current now.  Outside
+  // stream capture it is looked up on every call, so that a device reset or
+  // another context on the same device gets its own address; while the
+  // stream is being captured the address of the last eager call is used.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return na_fail(FLOF_E_CUDA, "calcLsDiff4d_noalloc: cannot query the stream");
+  }
   double *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
-      // set-up, once per device, with that device current
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_lsdiff_scratch) != cudaSuccess || !p) {
         cudaGetLastError();
@@ -117,19 +126,31 @@ extern "C" FLOF_API int flof_calcLsDiff4d_noalloc(const float *i0, const float *
     }
     scratch = g_scratch_ptr[dev];
   }
-  cudaStream_t s = (cudaStream_t)stream;
   // the arrival counter must start at zero; the partials are overwritten
   if (cudaMemsetAsync(scratch + NA_MAX_BLOCKS, 0, sizeof(double), s) != cudaSuccess)
     return na_fail(FLOF_E_CUDA, "calcLsDiff4d_noalloc: clearing the arrival counter failed");
   const Dims4 d{dims[0], dims[1], dims[2], dims[3]};
-  const long long nbox = (long long)ex * ey * ez * et;
-  const BoxDecoder bx = make_decoder(ex, ey, ez, bnd, bnd, bnd, bnd);
+  // Grid4d's is3D() and is4D() are constant true (grid4d.h:82-83): every
+  // axis loses 2 bnd cells.  A bnd that leaves none gives the reference's
+  // 0 * (1 / count), which one block computes.
+  const bool empty = ex <= 0 || ey <= 0 || ez <= 0 || et <= 0;
+  const long long nbox = empty ? 0 : (long long)ex * ey * ez * et;
+  const BoxDecoder bx = make_decoder(empty ? 1 : ex, empty ? 1 : ey, empty ? 1 : ez, bnd, bnd,
+                                     bnd, bnd);
   long long nb = (nbox + NA_THREADS - 1) / NA_THREADS;
   if (nb > NA_MAX_BLOCKS) nb = NA_MAX_BLOCKS;
+  if (nb < 1) nb = 1;
   const double scale = 1. / (double)(ex * ey * ez * et);
+  // an error the caller left pending is not ours to report or to clear
+  const cudaError_t before = cudaPeekAtLastError();
   k_ls_diff_noalloc<<<(int)nb, NA_THREADS, 0, s>>>(i0, i1, out, d, bx, (uint32_t)nbox, correction,
                                                    scale, scratch, result);
-  if (cudaGetLastError() != cudaSuccess)
-    return na_fail(FLOF_E_CUDA, "calcLsDiff4d_noalloc: kernel launch failed");
+  const cudaError_t after = cudaPeekAtLastError();
+  if (after != cudaSuccess && after != before) {
+    cudaGetLastError();
+    const std::string msg =
+        std::string("calcLsDiff4d_noalloc: kernel launch failed: ") + cudaGetErrorString(after);
+    return na_fail(FLOF_E_CUDA, msg.c_str());
+  }
   return FLOF_OK;
 }

@@ -290,8 +290,9 @@ __global__ void k_ls_diff(const float *__restrict__ i0, const float *__restrict_
   }
 }
 int ls_diff_blocks(Dims4 d, int bnd) {
-  long long nb = (long long)(d.x - 2 * bnd) * (d.y - 2 * bnd) * (d.z - 2 * bnd) * (d.t - 2 * bnd);
-  return grid_for(nb > 0 ? nb : 1, NT, 4);
+  const long long ex = d.x - 2 * bnd, ey = d.y - 2 * bnd, ez = d.z - 2 * bnd, et = d.t - 2 * bnd;
+  const long long nb = (ex > 0 && ey > 0 && ez > 0 && et > 0) ? ex * ey * ez * et : 1;
+  return grid_for(nb, NT, 4);
 }
 void launch_ls_diff(const float *i0, const float *i1, float *out, Dims4 d,
                     float correction, int bnd, double *partials,
@@ -300,7 +301,11 @@ void launch_ls_diff(const float *i0, const float *i1, float *out, Dims4 d,
   const int ex = d.x - 2 * bnd, ey = d.y - 2 * bnd, ez = d.z - 2 * bnd, et = d.t - 2 * bnd;
   long long nbox = (ex > 0 && ey > 0 && ez > 0 && et > 0) ? (long long)ex * ey * ez * et : 0;
   BoxDecoder bx = make_decoder(ex > 0 ? ex : 1, ey > 0 ? ey : 1, ez > 0 ? ez : 1, bnd, bnd, bnd, bnd);
-  // accu *= 1. / double(sx*sy*sz*st) with int arithmetic for the count
+  // accu *= 1. / double(sx*sy*sz*st) with int arithmetic for the count.
+  // Grid4d's is3D() and is4D() are constant true (grid4d.h:82-83), so
+  // FOR_IJKT_BND (kernel.h:62-68) and this count shrink every axis, T == 1
+  // included.  When bnd leaves no cells the loop adds nothing and the
+  // reference returns 0 * (1 / cnt): -0 for a negative count, NaN for 0.
   const int cnt = ex * ey * ez * et;
   const double scale = 1. / (double)cnt;
   k_ls_diff<<<ls_diff_blocks(d, bnd), NT, 0, s>>>(i0, i1, out, d, bx, (uint32_t)nbox,

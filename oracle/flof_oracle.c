@@ -611,8 +611,15 @@ typedef struct {
   REAL *blockd;     /* 4n */
 } ofmat;
 
+/* The element-wise loops of the PCG (applyMat, addScaled, precondApply,
+ * getMaxNorm) run their rows on OpenMP threads: each row is computed alone,
+ * and the signed maximum does not depend on the order, so the results are
+ * the serial loops' bit for bit.  dotProd stays one serial double sum, the
+ * reference's order. */
+
 /* applyMat (optflow4d.cpp:211-232) */
 static void apply_mat(const ofmat *A, const REAL *x, REAL *res) {
+#pragma omp parallel for schedule(static)
   for (idx_t i = 0; i < A->n; ++i) {
     REAL v = 0;
     const REAL od = A->offd[i];
@@ -630,15 +637,27 @@ static double dot_prod(const REAL *a, const REAL *b, idx_t n) {
   for (idx_t i = 0; i < n; ++i) d += a[i] * b[i];
   return d;
 }
-/* getMaxNorm (:243-250): signed maximum */
+/* getMaxNorm (:243-250): signed maximum.  Every thread starts from a[0]
+ * and keeps the same ">" rule, so NaN entries are skipped (and a NaN a[0]
+ * sticks) exactly as in the serial loop. */
 static REAL max_norm(const REAL *a, idx_t n) {
   REAL m = a[0];
-  for (idx_t i = 1; i < n; ++i)
-    if (a[i] > m) m = a[i];
+#pragma omp parallel
+  {
+    REAL mt = a[0];
+#pragma omp for schedule(static) nowait
+    for (idx_t i = 1; i < n; ++i)
+      if (a[i] > mt) mt = a[i];
+#pragma omp critical
+    {
+      if (mt > m) m = mt;
+    }
+  }
   return m;
 }
 /* addScaled (:253-258): a += (double)b * c, stored as REAL */
 static void add_scaled(REAL *a, double b, const REAL *c, idx_t n) {
+#pragma omp parallel for schedule(static)
   for (idx_t i = 0; i < n; ++i) a[i] += b * c[i];
 }
 
@@ -668,10 +687,12 @@ static int cg_solve(const ofmat *A, const REAL *rhs, REAL *result,
   {
     const double acc = accuracy * residual;
     const double resIni = residual;
+#pragma omp parallel for schedule(static)
     for (idx_t i = 0; i < n; ++i) {
       REAL diag = A->blockd[i * 4 + (i - (i / 4) * 4)];
       pre[i] = (REAL)(1. / diag);
     }
+#pragma omp parallel for schedule(static)
     for (idx_t i = 0; i < n; ++i) tmp[i] = res[i] * pre[i];
     double sigma = dot_prod(tmp, res, n);
     info->sigma0 = sigma;
@@ -695,6 +716,7 @@ static int cg_solve(const ofmat *A, const REAL *rhs, REAL *result,
         ok = 1;
         goto done;
       }
+#pragma omp parallel for schedule(static)
       for (idx_t i = 0; i < n; ++i) tmp[i] = res[i] * pre[i];
       double sigmaNew = dot_prod(tmp, res, n);
       double beta = sigmaNew / sigma;
@@ -744,6 +766,8 @@ static void of_assemble(dims4 d, const REAL *vel, const REAL *i0,
     }
   }
   const REAL dxf = (REAL)(1. / (2. * (double)mDx));
+  /* rows are independent: OpenMP over t as the reference's kernels */
+#pragma omp parallel for schedule(static)
   for (int t = 0; t < d.t; ++t)
     for (int k = 0; k < d.z; ++k)
       for (int j = 0; j < d.y; ++j)
@@ -1112,6 +1136,7 @@ typedef struct {
 } orc_ms_params;
 
 static void vadd(REAL *a, const REAL *b, idx_t n) {
+#pragma omp parallel for schedule(static)
   for (idx_t q = 0; q < n; ++q) a[q] += b[q];
 }
 

@@ -232,6 +232,24 @@ def test_corrvelsof_sparse_bitexact(gpu, orc):
     assert np.array_equal(gd.to_numpy(), want_dst)
 
 
+@pytest.mark.parametrize("dims,bnd", [((12, 10, 9, 1), 1), ((12, 10, 9, 1), 2), ((11, 10, 9, 3), 1),
+                                      ((9, 8, 7, 5), 3), ((12, 10, 9, 6), 0)])
+def test_calc_ls_diff_bounds_like_grid4d(gpu, orc, dims, bnd):
+    """Every axis loses 2 bnd cells, T == 1 included (Grid4d's is3D/is4D are
+    constant true, grid4d.h:82-83); a bnd that leaves no cells gives the
+    reference's 0 * (1 / count): -0 or NaN."""
+    r = np.random.default_rng(41)
+    X, Y, Z, T = dims
+    a = r.uniform(-1, 1, (T, Z, Y, X)).astype(np.float32)
+    b = r.uniform(-1, 1, (T, Z, Y, X)).astype(np.float32)
+    want = np.float32(orc.calcLsDiff4d(a, b, 0.7, bnd))
+    got = np.float32(F.calcLsDiff4d(grid_of(a), grid_of(b), None, 0.7, bnd))
+    if np.isnan(want):
+        assert np.isnan(got)
+    else:
+        assert got == want and np.signbit(got) == np.signbit(want), (got, want)
+
+
 FLOF = dict(wSmooth=0.001, wEnergy=0.0001, cgAccuracy=0.01, postVelBlur=4, cfl=999, multiStep=3,
             minGridSize=20, resetBndWidth=0.1)
 
@@ -275,6 +293,34 @@ def test_multiscale_flof_defaults(gpu, orc):
     assert [s[0] for s in st["solves"]] == [s[0] for s in wst]
     pre = orc.calcLsDiff4d(i0, i1, 0.1 / 20, 4)
     assert err < pre and abs(err - werr) <= 0.05 * pre
+
+
+def test_final_projection_decision_flips(gpu, orc):
+    """The 32^4 workload with flof's parameters, final projection on.  The
+    projection's line search and 4-cell cut-off decide per cell; from the
+    parallel PCG's field (within 1e-4 of the oracle's) some decisions can
+    flip.  The oracle's projectCells (knProjectCells, optflow4d.cpp:713-734)
+    runs on the oracle's and on the GPU's pre-projection fields, and the
+    fraction of cells whose decision (projected or not) differs is reported
+    and bounded.  With FLOF_OPT_STRICT the pipeline is bitwise instead
+    (tests/test_gpu_strict.py)."""
+    dims = (32, 32, 32, 32)
+    i0, i1 = drop_pair(dims)
+    zv = np.zeros(i0.shape + (4,), np.float32)
+    kw = dict(FLOF, doFinalProject=False)
+    want, _, _ = orc.opticalFlowMultiscale4d(zv, i0, i1, **kw)
+    got, _, _ = _gpu_multiscale(i0, i1, **kw)
+    _, mo = orc.projectCells(want, i0, i1, 4.0, 40)
+    _, mg = orc.projectCells(got, i0, i1, 4.0, 40)
+    box = (slice(2, -2),) * 4
+    flips = int(np.count_nonzero(mo[box] != mg[box]))
+    frac = flips / mo[box].size
+    # the whole pipeline with the projection, for the record
+    fw, _, _ = orc.opticalFlowMultiscale4d(zv, i0, i1, **dict(FLOF, doFinalProject=True))
+    fg, _, _ = _gpu_multiscale(i0, i1, **dict(FLOF, doFinalProject=True))
+    print(f"final projection: {flips} decision flips in {mo[box].size} cells ({frac:.2e}); "
+          f"pre-projection rel L2 {rel_l2(got, want):.2e}; with projection rel L2 {rel_l2(fg, fw):.2e}")
+    assert frac <= 1e-3
 
 
 def test_multiscale_cfl_substeps(gpu, orc):

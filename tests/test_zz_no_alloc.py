@@ -1,5 +1,6 @@
 """flof_calcLsDiff4d_noalloc, the entry point for callers that cannot
-allocate device memory (stream capture, fixed device-memory budgets).
+allocate device memory (fixed device-memory budgets, loops that cannot
+afford the device synchronisation an allocation may cost).
 
 It is called through the C ABI on buffers the caller allocated (torch
 tensors here) and must give what the context-based flof_calcLsDiff4d gives,
@@ -65,8 +66,14 @@ def test_calc_ls_diff_noalloc_matches_context_entry_point():
     torch.cuda.synchronize()
     assert abs(np.float32(tres.item()) - want) <= np.spacing(want)
 
-    # sizes beyond what the entry point handles are rejected with a message
+    # a bnd that leaves no cells: the reference's 0 * (1 / count), here
+    # count 0 (NaN), as the context entry point gives
     st = lib.flof_calcLsDiff4d_noalloc(_ptr(t0), _ptr(t1), None, cd, corr, 20, _ptr(tres), stream)
+    assert st == 0, lib.flof_last_error()
+    torch.cuda.synchronize()
+    assert np.isnan(tres.item()) and np.isnan(F.calcLsDiff4d(g0, g1, None, corr, 20))
+    # sizes beyond what the entry point handles are rejected with a message
+    st = lib.flof_calcLsDiff4d_noalloc(_ptr(t0), _ptr(t1), None, cd, corr, -1, _ptr(tres), stream)
     assert st == 1 and b"bnd" in lib.flof_last_error()
     big = (ctypes.c_int * 4)(2048, 2048, 1024, 2)
     st = lib.flof_calcLsDiff4d_noalloc(_ptr(t0), _ptr(t1), None, big, corr, 0, _ptr(tres), stream)
