@@ -68,7 +68,15 @@ def _args(**kw):
 def test_reference_arm_reports_from_rank_zero_only(monkeypatch, capsys):
     sys.path.insert(0, ROOT)
     import bench
-    monkeypatch.setattr(bench, "cpu_sample_seconds", lambda acc: 2.0)
+    class FakeCpu:
+        def __init__(self, R, H, acc):
+            assert (R, H) == (64, 128)
+            self.parts = {"solves_s": 3.0}
+
+        def step(self):
+            return 4.0
+
+    monkeypatch.setattr(bench, "CpuWorkload", FakeCpu)
     monkeypatch.setenv("WORLD_SIZE", "2")
     monkeypatch.setenv("RANK", "1")
     monkeypatch.setenv("LOCAL_RANK", "1")
@@ -81,7 +89,9 @@ def test_reference_arm_reports_from_rank_zero_only(monkeypatch, capsys):
     assert len(out) == 1
     line = json.loads(out[0])
     assert line["impl"] == "reference"
-    assert line["value"] == pytest.approx(1.0 / 32.0)  # 1 / (16 * 2 s)
+    assert line["value"] == pytest.approx(2.0 / 4.0)  # two solves per whole step
+    # one whole step, reported as run (the driver's step counts ask for more)
+    assert line["steps"] == 1 and line["warmup"] == 0 and line["ms_per_step"] == 4000.0
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["config"] == bench.flof_config(_args(), 2)
     assert line["metric"] == bench.METRIC and line["higher_is_better"] is True
