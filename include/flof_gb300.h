@@ -52,8 +52,11 @@ typedef enum { FLOF_REAL = 1, FLOF_VEC4 = 8 } flof_elem;
 /* Gaussian blur variants for postVelBlur (optflow4d.cpp:531-541).
  * 1 = the reference's direct 4D stencil (knGaussianBlur, :132-158), bitwise
  *     equal to the reference;
- * 2 = separable 4x1D stencil with the same in-bounds normalisation, equal
- *     to 1 up to float rounding and several times cheaper. */
+ * 2 = separable stencils: the blur as a 4x1D stencil with the same in-bounds
+ *     normalisation, and the projection's extrapolation sweep
+ *     (knCvExpolBlur4d, :613-626) with its 3^4 box sum formed as 3x3 (x,y)
+ *     sums added over z and t; equal to 1 up to float rounding and several
+ *     times cheaper. */
 enum { FLOF_BLUR_GAUSS = 1, FLOF_BLUR_GAUSS_SEPARABLE = 2 };
 
 typedef struct flof_ctx flof_ctx;
@@ -88,9 +91,16 @@ typedef struct flof_of_params {
    * flof_ctx_set_model (dropped when it does not lower that level's error
    * metric); 0 (default): the reference's zero start. */
   int warmStart;
-  int reserved[5];
+  /* FLOF_SOLVER_PCG (default): the reference's Jacobi-preconditioned CG.
+   * FLOF_SOLVER_MG: the same CG preconditioned by a multigrid V-cycle with
+   * the same stop rule on the same residual; the plain operator re-forms the
+   * final residual and the plain Jacobi-PCG finishes the solve when it is
+   * above the threshold (no reference counterpart). */
+  int solver;
+  int reserved[4];
 } flof_of_params;
 enum { FLOF_PRECISION_FP32 = 0, FLOF_PRECISION_MIXED = 1 };
+enum { FLOF_SOLVER_PCG = 0, FLOF_SOLVER_MG = 1 };
 
 #define FLOF_MAX_SOLVE_STATS 64
 /* Per-call record of the linear solves (the reference logs the same facts
@@ -164,6 +174,19 @@ FLOF_API const char *flof_kernel_class_name(int cls);
  *   0 (default): the parallel kernels. */
 enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3, FLOF_OPT_STRICT = 4 };
 FLOF_API int flof_ctx_set_option(flof_ctx *ctx, int option, int value);
+/* Parameters of the multigrid V-cycle of FLOF_SOLVER_MG (no reference
+ * counterpart): damping of the block-Jacobi sweeps on the system's own grid
+ * (omega0) and on the coarse levels (omegac), in (0, 1]; the scale of each
+ * coarse level's Laplacian against its Galerkin product (lambda, in
+ * (0, 1]; 1/2 rediscretises it); sweeps on the coarsest level (1..256);
+ * preconditioned iterations before the plain Jacobi-PCG takes over (>= 0).
+ * Defaults 0.95, 1.0, 0.9, 8, 200 (fitted on solver-generated systems). */
+FLOF_API int flof_ctx_set_mg_params(flof_ctx *ctx, float omega0, float omegac, float lambda,
+                                    int coarse_sweeps, int max_iter);
+/* Solves of FLOF_SOLVER_MG so far whose result the plain Jacobi-PCG had to
+ * finish (residual above the threshold, or no convergence within the
+ * preconditioned solve's iteration cap). */
+FLOF_API long long flof_ctx_mg_fallbacks(flof_ctx *ctx);
 /* Release cached device buffers of the context's pool (and its workers'). */
 FLOF_API int flof_ctx_trim(flof_ctx *ctx);
 

@@ -19,6 +19,8 @@ FLOF_OPT_AUTOTUNE = 3
 FLOF_OPT_STRICT = 4
 FLOF_PRECISION_FP32 = 0
 FLOF_PRECISION_MIXED = 1
+FLOF_SOLVER_PCG = 0
+FLOF_SOLVER_MG = 1
 MAX_SOLVE_STATS = 64
 
 STATUS = {
@@ -43,7 +45,8 @@ class OFParams(ctypes.Structure):
         ("resetBndWidth", ctypes.c_float), ("multiStep", ctypes.c_int),
         ("projSizeThresh", ctypes.c_int), ("minGridSize", ctypes.c_int),
         ("doFinalProject", ctypes.c_int), ("cgMaxIter", ctypes.c_int),
-        ("precision", ctypes.c_int), ("warmStart", ctypes.c_int), ("reserved", ctypes.c_int * 5),
+        ("precision", ctypes.c_int), ("warmStart", ctypes.c_int), ("solver", ctypes.c_int),
+        ("reserved", ctypes.c_int * 4),
     ]
 
 
@@ -100,6 +103,8 @@ SIGNATURES = {
     "flof_ctx_kernel_launches": (ctypes.c_longlong, [P]),
     "flof_ctx_trim": (I, [P]),
     "flof_ctx_set_option": (I, [P, I, I]),
+    "flof_ctx_set_mg_params": (I, [P, F, F, F, I, I]),
+    "flof_ctx_mg_fallbacks": (ctypes.c_longlong, [P]),
     "flof_ctx_profile": (I, [P, I]),
     "flof_ctx_profile_count": (I, [P, IP]),
     "flof_ctx_profile_record": (I, [P, I, IP, IP, ctypes.POINTER(ctypes.c_double), FP]),

@@ -106,6 +106,16 @@ class Context:
         """flof_ctx_set_option, e.g. _lib.FLOF_OPT_CFL_SYNC."""
         check(self.lib.flof_ctx_set_option(self.h, int(option), int(value)))
 
+    def set_mg_params(self, omega0=0.95, omegac=1.0, lam=0.9, coarse_sweeps=8, max_iter=200):
+        """flof_ctx_set_mg_params: the V-cycle of solver="mg" and its
+        iteration cap before the plain PCG takes over."""
+        check(self.lib.flof_ctx_set_mg_params(self.h, float(omega0), float(omegac), float(lam),
+                                              int(coarse_sweeps), int(max_iter)))
+
+    def mg_fallbacks(self) -> int:
+        """Solves of solver="mg" that the plain PCG had to finish."""
+        return int(self.lib.flof_ctx_mg_fallbacks(self.h))
+
     def profile(self, enable: bool = True):
         """Start (clearing old records) or stop per-launch event tracing."""
         check(self.lib.flof_ctx_profile(self.h, int(bool(enable))))
@@ -397,7 +407,8 @@ def _ctx_of(g) -> Context:
 
 def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e-04, blurType=1, cfl=999,
                orderTime=1, orderSpace=1, resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999,
-               minGridSize=10, doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False):
+               minGridSize=10, doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False,
+               solver="pcg"):
     p = OFParams()
     _lib.lib().flof_of_params_default(ctypes.byref(p))
     p.wSmooth, p.wEnergy, p.level = wSmooth, wEnergy, int(level)
@@ -411,22 +422,29 @@ def _of_params(wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0, cgAccuracy=1e
         raise FlofError(1, "precision must be 'fp32' or 'mixed'")
     p.precision = prec[precision]
     p.warmStart = int(bool(warmStart))
+    solvers = {"pcg": _lib.FLOF_SOLVER_PCG, "mg": _lib.FLOF_SOLVER_MG}
+    if solver not in solvers:
+        raise FlofError(1, "solver must be 'pcg' or 'mg'")
+    p.solver = solvers[solver]
     return p
 
 
 def opticalFlowMultiscale4d(vel, i0, i1, rhsT=None, wSmooth=0.0, wEnergy=0.0, level=0, postVelBlur=0.0,
                             cgAccuracy=1e-04, blurType=1, cfl=999, orderTime=1, orderSpace=1,
                             resetBndWidth=-1.0, multiStep=1, projSizeThresh=9999, minGridSize=10,
-                            doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False):
+                            doFinalProject=False, cgMaxIter=1000, precision="fp32", warmStart=False,
+                            solver="pcg"):
     """opticalFlowMultiscale4d (optflow4d.cpp:2182-2195); returns the final
     error metric (the reference's template returns it to C++ callers).
+    solver="mg" preconditions the CG with a multigrid V-cycle (same stop
+    rule; the plain PCG judges and finishes);
     precision="mixed" solves with the BF16-stored gradient and FP64
     iterative refinement; warmStart=True starts the coarsest level from the
     model attached with Model.attach (neither has a reference counterpart)."""
     global _last_stats
     p = _of_params(wSmooth, wEnergy, level, postVelBlur, cgAccuracy, blurType, cfl, orderTime, orderSpace,
                    resetBndWidth, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter,
-                   precision, warmStart)
+                   precision, warmStart, solver)
     err = ctypes.c_float()
     st = SolveStats()
     ctx = _ctx_of(vel)

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libflof_gb300.so")
 SOURCES = ["flof_ops.cu", "flof_solve.cu", "flof_stencil.cu", "flof_tma.cu", "flof_cond.cu",
            "flof_host.cu", "flof_ext.cu", "flof_uni.cu", "flof_batch.cu", "flof_mixed.cu",
            "flof_net.cu", "flof_conv_tc.cu", "flof_model.cu", "flof_noalloc.cu",
-           "flof_strict.cu"]
+           "flof_strict.cu", "flof_mg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -28,6 +28,8 @@ flof_ctx *worker(flof_ctx *c, size_t q) {
     if (flof_ctx_create(c->device, &w) != FLOF_OK) fail(FLOF_E_CUDA, g_last_error);
     w->cfl_force_sync = c->cfl_force_sync;
     w->autotune = c->autotune;
+    w->strict = c->strict;
+    w->mg = c->mg;
     w->tune_owner = c;
     c->workers.push_back(w);
   }

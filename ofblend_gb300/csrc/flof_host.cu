@@ -195,6 +195,7 @@ struct OFArgs {
   float wSmooth, wEnergy, postVelBlur, cgAccuracy, resetBndWidth;
   int blurType, cgMaxIter;
   int precision = FLOF_PRECISION_FP32;
+  int solver = FLOF_SOLVER_PCG;
 };
 
 // opticalFlowDim<Grid4d<Real>,Grid4d<Vec4>,4> (optflow4d.cpp:361-553).
@@ -351,6 +352,104 @@ void pcg_loop_strict(flof_ctx *c, Dims4 d, const OFConsts &k, float4 *x, float4 
   }
 }
 
+// Multigrid-preconditioned PCG (solver FLOF_SOLVER_MG, flof_mg.cu) from the
+// state the assembly left (x = 0, r = b, resIni = signed max of b, acc =
+// cgAccuracy * resIni): the stop rule is the reference's, on the same
+// residual.  The plain operator then judges the result: r = b - A x is
+// formed anew (FP64 row sums) and, when its signed max is above the same
+// threshold, or the preconditioned solve did not converge within its
+// iteration cap, the plain Jacobi-PCG continues from x to that threshold.
+// Returns the status; *iters counts both solvers' iterations.
+int mg_pcg(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, const OFArgs &a, float4 *x,
+           float4 *r, float4 *p, float4 *q, const float4 *g, const float *i1, int *iters,
+           float *res) {
+  const size_t vb = vec_bytes(d);
+  const std::vector<Dims4> dims = mg_level_dims(d);
+  const int nl = (int)dims.size();
+  std::vector<DBuf> bufs;
+  std::vector<MGLevelPtrs> L(nl);
+  for (int l = 0; l < nl; ++l) {
+    const size_t n = (size_t)dims[l].cells();
+    auto take = [&](size_t nf4) {
+      bufs.emplace_back(c, nf4 * sizeof(float4));
+      return bufs.back().v();
+    };
+    L[l].m = dims[l];
+    L[l].G = take(3 * n);
+    L[l].dinv = take(3 * n);
+    L[l].cpl = take(n);
+    L[l].b = take(n);
+    L[l].x = take(n);
+    L[l].r = take(n);
+  }
+  DBuf x0(c, vb), r0(c, vb), z(c, vb), b(c, vb);
+  CK(cudaMemcpyAsync(b.p, r, vb, cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaMemsetAsync(x0.p, 0, vb, c->stream));  // its border stays zero
+  MGParams mp = c->mg;
+  const double nb = (double)nint(d);
+  KLP(c, KC_MG, d.x, nb * 16, launch_mg_build(g, d, L.data(), nl, k, mp, c->st, c->stream));
+  int vl = nl > 1 ? nl - 1 : 0;  // the build's launches beyond the one counted
+  KLP(c, KC_MG, d.x, nb * 96,
+      launch_mg_vcycle(r, g, x0.v(), r0.v(), z.v(), d, L.data(), nl, k, mp, c->st, c->dpart, 1, 0,
+                       c->stream, &vl));
+  KLP(c, KC_DIRECTION, d.x, nb * 32, launch_mgcg_direction(p, z.v(), d, c->st, 1, c->stream));
+  const int cap = a.cgMaxIter < mp.max_iter ? a.cgMaxIter : mp.max_iter;
+  int it = 0, chunk = 2;
+  for (;;) {
+    const int n = (cap - it) < chunk ? (cap - it) : chunk;
+    for (int s = 0; s < n; ++s) {
+      KLP(c, KC_MATVEC, d.x, nb * 48, launch_cg_matvec(p, g, q, d, k, c->st, c->dpart, c->stream, tu));
+      KLP(c, KC_UPDATE, d.x, nb * 128,
+          launch_mgcg_update_pre(x, r, p, q, g, x0.v(), d, k, mp, c->st, c->fpart, cap,
+                                 c->stream));
+      KLP(c, KC_MG, d.x, nb * 128,
+          launch_mg_vcycle(r, g, x0.v(), r0.v(), z.v(), d, L.data(), nl, k, mp, c->st, c->dpart, 0,
+                           1, c->stream, &vl));
+      KLP(c, KC_DIRECTION, d.x, nb * 48, launch_mgcg_direction(p, z.v(), d, c->st, 0, c->stream));
+    }
+    it += n;
+    CK(cudaMemcpyAsync(c->st_h, c->st, sizeof(CGState), cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+    if (c->st_h->done != CG_RUNNING || it >= cap) break;
+    chunk = chunk * 2 > 16 ? 16 : chunk * 2;
+  }
+  c->launches += vl;
+  int status = c->st_h->done;
+  if (status == CG_RUNNING) status = CG_MAXITER;
+  int total = c->st_h->iters;
+  float ret = c->st_h->retResidual;
+  if (status == CG_CONVERGED || status == CG_MAXITER) {
+    // the plain operator judges the result
+    const double bmax = c->st_h->resIni;
+    const double goal = (double)a.cgAccuracy * bmax;
+    KLP(c, KC_MG, d.x, nb * 64,
+        launch_mg_judge(x, b.v(), g, r, d, k, c->fpart, c->counter + 7, c->fres + 8, c->stream));
+    CK(cudaMemcpyAsync(c->fres_h + 10, c->fres + 8, sizeof(float), cudaMemcpyDeviceToHost,
+                       c->stream));
+    sync(c);
+    const double rmax = (double)c->fres_h[10];
+    ret = (float)(rmax / bmax);
+    if (rmax > goal) {
+      // the plain Jacobi-PCG finishes from x, to the same absolute threshold
+      const float acc_rel = (float)(goal / rmax);
+      KLP(c, KC_ASSEMBLE, d.x, nb * 40,
+          launch_cg_init_r(r, g, p, d, k, acc_rel, c->st, c->dpart, c->fpart, c->stream));
+      pcg_loop(c, d, k, tu, x, r, p, q, g, a.cgMaxIter, i1);
+      status = c->st_h->done;
+      if (status == CG_RUNNING) status = CG_MAXITER;
+      if (status == CG_EARLY) status = CG_CONVERGED;
+      total += c->st_h->iters;
+      ret = (float)((double)c->st_h->resMax / bmax);
+      c->mg_fallbacks++;
+    } else {
+      status = CG_CONVERGED;
+    }
+  }
+  if (iters) *iters = total;
+  if (res) *res = ret;
+  return status;
+}
+
 // Mixed-precision solve with iterative refinement.  The PCG runs on the
 // matrix of the BF16-stored gradient, first to sqrt(cgAccuracy) (restarting
 // from the assembly's r = b with that matrix's preconditioner).  Then, up to
@@ -437,7 +536,14 @@ void optical_flow_dim(flof_ctx *c, Dims4 d, float4 *velOut, const float4 *velIn,
   KLP(c, KC_ASSEMBLE, d.x, nint(d) * 8 + d.cells() * 64,
       launch_of_assemble_init(i0w, i1, velIn, g.v(), r.v(), p.v(), x.v(), d, k,
                                 a.cgAccuracy, c->st, c->dpart, c->fpart, c->stream));
-  if (a.precision != FLOF_PRECISION_MIXED) {
+  if (a.solver == FLOF_SOLVER_MG && a.precision != FLOF_PRECISION_MIXED && !c->strict) {
+    int iters = 0;
+    float res = 0.f;
+    const int status = mg_pcg(c, d, k, tu, a, x.v(), r.v(), p.v(), q.v(), g.v(), i1, &iters, &res);
+    record_solve(c, d.x, iters, res, status);
+    if (itersOut) *itersOut = iters;
+    if (resOut) *resOut = res;
+  } else if (a.precision != FLOF_PRECISION_MIXED) {
     if (c->strict)
       pcg_loop_strict(c, d, k, x.v(), r.v(), p.v(), q.v(), g.v(), a.cgMaxIter);
     else
@@ -508,7 +614,8 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       bool tma = false;
       KLP(c, KC_EXPOL, d.x, d.cells() * 32,
           tma = launch_expol_tma(A, B, (const uint16_t *)mask.p, track ? fA : nullptr,
-                                 track ? fB : nullptr, fKeep, d, c->dev_err, c->stream));
+                                 track ? fB : nullptr, fKeep, d, c->dev_err, c->stream,
+                                 blurType == FLOF_BLUR_GAUSS_SEPARABLE));
       if (!tma) {
         // the flags no longer describe the buffers once a sweep runs untracked
         track = false;
@@ -545,6 +652,7 @@ struct MSArgs {
   int blurType, multiStep, projSizeThresh, minGridSize, doFinalProject, cgMaxIter;
   int precision = FLOF_PRECISION_FP32;
   int warmStart = 0;
+  int solver = FLOF_SOLVER_PCG;
 };
 
 // opticalFlowMultiscaleTemplate (optflow4d.cpp:936-1173).
@@ -563,6 +671,7 @@ float multiscale(flof_ctx *c, Dims4 d, float4 *vel, const float *i0, const float
   oa.blurType = p.blurType;
   oa.cgMaxIter = p.cgMaxIter;
   oa.precision = p.precision;
+  oa.solver = p.solver;
 
   DBuf i0warped(c, real_bytes(d));
   CK(cudaMemcpyAsync(i0warped.p, i0, real_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
@@ -917,6 +1026,26 @@ FLOF_API int flof_ctx_set_option(flof_ctx *c, int option, int value) {
   });
 }
 
+FLOF_API int flof_ctx_set_mg_params(flof_ctx *c, float omega0, float omegac, float lambda,
+                                    int coarse_sweeps, int max_iter) {
+  return guarded([&] {
+    need(c != nullptr, "ctx is NULL");
+    need(omega0 > 0.f && omega0 <= 1.f && omegac > 0.f && omegac <= 1.f,
+         "the damping factors must be in (0, 1]");
+    need(lambda > 0.f && lambda <= 1.f, "lambda must be in (0, 1]");
+    need(coarse_sweeps >= 1 && coarse_sweeps <= 256, "coarse_sweeps must be in 1..256");
+    need(max_iter >= 0, "max_iter must be >= 0");
+    c->mg.max_iter = max_iter;
+    c->mg.omega0 = omega0;
+    c->mg.omegac = omegac;
+    c->mg.lambda = lambda;
+    c->mg.coarse_sweeps = coarse_sweeps;
+    for (flof_ctx *w : c->workers) w->mg = c->mg;
+  });
+}
+
+FLOF_API long long flof_ctx_mg_fallbacks(flof_ctx *c) { return c ? c->mg_fallbacks : 0; }
+
 FLOF_API int flof_ctx_trim(flof_ctx *c) {
   return guarded([&] {
     need(c != nullptr, "ctx is NULL");
@@ -1229,6 +1358,8 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     need(pp.cfl > 0.f, "cfl must be positive");
     need(pp.precision == FLOF_PRECISION_FP32 || pp.precision == FLOF_PRECISION_MIXED,
          "precision must be FLOF_PRECISION_FP32 or FLOF_PRECISION_MIXED");
+    need(pp.solver == FLOF_SOLVER_PCG || pp.solver == FLOF_SOLVER_MG,
+         "solver must be FLOF_SOLVER_PCG or FLOF_SOLVER_MG");
     set_ctx_device(c);
     const auto t0 = std::chrono::steady_clock::now();
     flof_solve_stats local;
@@ -1251,6 +1382,7 @@ FLOF_API int flof_opticalFlowMultiscale4d(flof_ctx *c, flof_grid *vel, const flo
     m.cgMaxIter = pp.cgMaxIter;
     m.precision = pp.precision;
     m.warmStart = pp.warmStart;
+    m.solver = pp.solver;
     float e;
     try {
       // speculative pass: CFL substep counts checked on the device

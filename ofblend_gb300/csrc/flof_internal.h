@@ -98,12 +98,13 @@ struct Pool {
 enum KClass {
   KC_OTHER = 0, KC_ASSEMBLE, KC_MATVEC, KC_UPDATE, KC_DIRECTION, KC_COPYBACK, KC_BLUR,
   KC_PROJECT, KC_EXPOL, KC_ADVECT, KC_RESAMPLE, KC_LSDIFF, KC_REDUCE, KC_ELEMWISE, KC_BORDER,
-  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_EXPOL_MASK, KC_COUNT
+  KC_LOOKUP, KC_DEFORM, KC_BLEND, KC_EXPOL_MASK, KC_MG, KC_COUNT
 };
 inline const char *kc_names[KC_COUNT] = {
     "other", "of_assemble_init", "cg_matvec", "cg_update", "cg_direction", "of_copy_back",
     "gauss_blur", "project_cells", "expol_sweep", "advect", "resample", "ls_diff", "reduce",
-    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices", "expol_mask"};
+    "elementwise", "border", "lookup_slice", "deform_twoway", "blend_slices", "expol_mask",
+    "mg_vcycle"};
 
 struct ProfRec {
   int cls;
@@ -155,6 +156,10 @@ struct flof_ctx {
   int autotune = 0;
   // FLOF_OPT_STRICT: the reference's PCG and error-metric arithmetic
   int strict = 0;
+  // parameters of the multigrid preconditioner (FLOF_SOLVER_MG) and the
+  // number of its solves the plain PCG had to finish
+  flof::MGParams mg;
+  long long mg_fallbacks = 0;
   std::map<std::array<int, 4>, flof::CGTune> tunes;
   std::mutex tune_mu;
   flof_ctx *tune_owner = nullptr;

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "flof_common.cuh"
 
 namespace flof {
@@ -173,6 +175,59 @@ void launch_strict_iteration(float4 *x, float4 *r, float4 *p, float4 *q, const f
 // calcLsDiffTempl with the serial double sum in the reference's loop order.
 void launch_strict_ls_diff(const float *i0, const float *i1, float *out, Dims4 d, float correction,
                            int bnd, double *result_d, float *result_f, cudaStream_t s);
+// ---- multigrid-preconditioned PCG (flof_mg.cu) --------------------------------
+// Parameters of the V-cycle: damping of the block-Jacobi sweeps on level 0
+// and on the coarse levels, the scale of each coarse level's Laplacian
+// against its Galerkin product (1/2: rediscretised), and the sweeps on the
+// coarsest level.  The defaults are the fit of ofblend_gb300/mgfit.py on six
+// seeded 32^4 drop pairs at cgAccuracy 1e-4 (290 -> 213 iterations against
+// 0.8 / 0.8 / 0.5 / 24).
+struct MGParams {
+  float omega0 = 0.95f;
+  float omegac = 1.0f;
+  float lambda = 0.9f;
+  int coarse_sweeps = 8;
+  int max_iter = 200;  // preconditioned iterations before the plain PCG takes over
+};
+// One coarse level: dense dims m; G (3 float4 per cell: the summed
+// g g^T + wEnergy block and lapdiag), couplings to the +a neighbours, the
+// block inverse (3 float4 per cell), and the V-cycle's rhs, iterate and
+// scratch vectors (x and r are swapped by the V-cycle).
+struct MGLevelPtrs {
+  Dims4 m;
+  float4 *G, *cpl, *dinv, *b, *x, *r;
+};
+// Dims of the coarse levels of a system on grid d (interior cells
+// aggregated 2^4 at a time until at most 1024 cells remain); empty for a
+// grid without interior cells.
+std::vector<Dims4> mg_level_dims(Dims4 d);
+// Builds the coarse operators from the level-0 gradient g.
+void launch_mg_build(const float4 *g, Dims4 d, const MGLevelPtrs *L, int nl, const OFConsts &c,
+                     const MGParams &mp, const CGState *st, cudaStream_t s);
+// z = V-cycle(b0) on level 0 (x0, r0: level-0 scratch, x0's border zero),
+// plus z.b0 into the PCG state: init 1 sets sigma (and beta = 0), init 0
+// sets beta = z.b0 / sigma and sigma.  Counts its launches into *launches.
+// pre_done: x0 already holds the first level-0 sweep (launch_mgcg_update_pre).
+void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0, float4 *z, Dims4 d,
+                      MGLevelPtrs *L, int nl, const OFConsts &c, const MGParams &mp, CGState *st,
+                      double *dpart, int init, int pre_done, cudaStream_t s, int *launches);
+// x += alpha p, r -= alpha q, signed max of r and the stop rule.
+void launch_mgcg_update(float4 *x, float4 *r, const float4 *p, const float4 *q, Dims4 d,
+                        CGState *st, float *fpart, int maxIter, cudaStream_t s);
+// The same plus the V-cycle's first level-0 sweep x0 = omega0 D^-1 r.
+void launch_mgcg_update_pre(float4 *x, float4 *r, const float4 *p, const float4 *q,
+                            const float4 *g, float4 *x0, Dims4 d, const OFConsts &c,
+                            const MGParams &mp, CGState *st, float *fpart, int maxIter,
+                            cudaStream_t s);
+// The plain operator's residual r = b - A x of a preconditioned solve (float
+// rows) and its signed maximum into the device float *rmax.
+void launch_mg_judge(const float4 *x, const float4 *b, const float4 *g, float4 *r, Dims4 d,
+                     const OFConsts &c, float *fpart, unsigned int *counter, float *rmax,
+                     cudaStream_t s);
+// p = z + beta p (init: p = z).
+void launch_mgcg_direction(float4 *p, const float4 *z, Dims4 d, const CGState *st, int init,
+                           cudaStream_t s);
+
 // ---- mixed precision (flof_mixed.cu) ------------------------------------------
 // g16 = bf16(g) over n cells
 void launch_to_bf4(const float4 *g, BF4 *g16, long long n, cudaStream_t s);
@@ -187,6 +242,8 @@ void launch_residual64(const float4 *x, const float4 *b, const float4 *g, float4
 // M^-1 r on the interior, sigma = z.r, resIni = signed max of r; the state
 // logic of the assembly's initialisation.
 void launch_cg_init_r(const float4 *r, const BF4 *g, float4 *p, Dims4 d, OFConsts c,
+                      float accuracy, CGState *st, double *dpart, float *fpart, cudaStream_t s);
+void launch_cg_init_r(const float4 *r, const float4 *g, float4 *p, Dims4 d, OFConsts c,
                       float accuracy, CGState *st, double *dpart, float *fpart, cudaStream_t s);
 // x = float((double)x + (double)e) over n cells
 void launch_add_correction(float4 *x, const float4 *e, long long n, cudaStream_t s);
@@ -246,9 +303,11 @@ size_t expol_tiles(Dims4 d);
 void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
                        uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st);
 // nz_in / nz_out: the flags of the in and out buffers (null: no skipping).
+// separable: the 3^4 box sum formed as 3x3 (x,y) slab sums added over z and
+// t (blurType 2), equal to the reference's 81-term sum up to rounding.
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
                       uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
-                      cudaStream_t st);
+                      cudaStream_t st, bool separable = false);
 
 // ---- projection correction ------------------------------------------------------
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,

@@ -117,8 +117,9 @@ k_residual64(const float4 *__restrict__ x, const float4 *__restrict__ b,
 
 // PCG start from residual r with x0 = 0 (x zeroed by the caller): p = z on
 // the interior; the state logic of k_of_assemble_init.
+template <class GT>
 __global__ void __launch_bounds__(NT)
-k_cg_init_r(const float4 *__restrict__ r, const BF4 *__restrict__ g, float4 *__restrict__ p,
+k_cg_init_r(const float4 *__restrict__ r, const GT *__restrict__ g, float4 *__restrict__ p,
             Dims4 d, BoxDecoder bx, uint32_t nint, OFConsts c, float accuracy, CGState *st,
             double *dpart, float *fpart) {
   __shared__ double shd[NT / 32];
@@ -220,6 +221,12 @@ void launch_residual64(const float4 *x, const float4 *b, const float4 *g, float4
 }
 
 void launch_cg_init_r(const float4 *r, const BF4 *g, float4 *p, Dims4 d, OFConsts c,
+                      float accuracy, CGState *st, double *dpart, float *fpart, cudaStream_t s) {
+  const uint32_t n = interior_count(d);
+  k_cg_init_r<<<grid_for(n > 0 ? n : 1, NT, 8), NT, 0, s>>>(r, g, p, d, interior_decoder(d), n, c,
+                                                           accuracy, st, dpart, fpart);
+}
+void launch_cg_init_r(const float4 *r, const float4 *g, float4 *p, Dims4 d, OFConsts c,
                       float accuracy, CGState *st, double *dpart, float *fpart, cudaStream_t s) {
   const uint32_t n = interior_count(d);
   k_cg_init_r<<<grid_for(n > 0 ? n : 1, NT, 8), NT, 0, s>>>(r, g, p, d, interior_decoder(d), n, c,
