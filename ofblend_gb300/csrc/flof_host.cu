@@ -589,6 +589,7 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
   DBuf mask(c, expol_mask_words(d) * sizeof(uint16_t));
   const size_t ntiles = expol_tiles(d);
   DBuf tflags(c, 3 * ntiles * sizeof(uint32_t));  // zero tracking: buffer A, buffer B, kept
+  DBuf s2;  // the separable sweep's (x,y) box sums (blurType 2)
   int singleStep = 0;
   if (postVelBlur < blurThreshold) singleStep = 1;
   float4 *A = dst;
@@ -606,16 +607,24 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       // The sweeps only rewrite unmarked interior cells; both buffers carry
       // the projected values everywhere else (the reference's tmp copy).
       CK(cudaMemcpyAsync(B, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
-      CK(cudaMemsetAsync(tflags.p, 0, 3 * ntiles * sizeof(uint32_t), c->stream));
-      KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 20,
-          launch_expol_mask(marker.f(), A, (uint16_t *)mask.p, fA, fB, fKeep, d, c->stream));
+      if (blurType != FLOF_BLUR_GAUSS_SEPARABLE) {  // the separable sweep reads the marker
+        CK(cudaMemsetAsync(tflags.p, 0, 3 * ntiles * sizeof(uint32_t), c->stream));
+        KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 20,
+            launch_expol_mask(marker.f(), A, (uint16_t *)mask.p, fA, fB, fKeep, d, c->stream));
+      }
     }
     for (int s = 0; s < doCvExtrapol; ++s) {
+      if (blurType == FLOF_BLUR_GAUSS_SEPARABLE) {
+        if (!s2.p) s2 = DBuf(c, vec_bytes(d));
+        KLP(c, KC_EXPOL, d.x, d.cells() * 68,
+            launch_expol_sep(A, B, s2.v(), marker.f(), d, c->stream));
+        std::swap(A, B);
+        continue;
+      }
       bool tma = false;
       KLP(c, KC_EXPOL, d.x, d.cells() * 32,
           tma = launch_expol_tma(A, B, (const uint16_t *)mask.p, track ? fA : nullptr,
-                                 track ? fB : nullptr, fKeep, d, c->dev_err, c->stream,
-                                 blurType == FLOF_BLUR_GAUSS_SEPARABLE));
+                                 track ? fB : nullptr, fKeep, d, c->dev_err, c->stream));
       if (!tma) {
         // the flags no longer describe the buffers once a sweep runs untracked
         track = false;

@@ -303,11 +303,15 @@ size_t expol_tiles(Dims4 d);
 void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
                        uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st);
 // nz_in / nz_out: the flags of the in and out buffers (null: no skipping).
-// separable: the 3^4 box sum formed as 3x3 (x,y) slab sums added over z and
-// t (blurType 2), equal to the reference's 81-term sum up to rounding.
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
                       uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
-                      cudaStream_t st, bool separable = false);
+                      cudaStream_t st);
+// The sweep with its 3^4 box sum formed separably (blurType 2, flof_mg.cu):
+// s2 (a Vec4 grid of d's size) receives the 3x3 (x,y) sums, out the 1/81 of
+// their 3x3 (z,t) sums at unmarked interior cells.  Equal to the reference's
+// 81-term sum up to rounding.
+void launch_expol_sep(const float4 *in, float4 *out, float4 *s2, const float *mark, Dims4 d,
+                      cudaStream_t s);
 
 // ---- projection correction ------------------------------------------------------
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,

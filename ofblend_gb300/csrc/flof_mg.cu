@@ -134,6 +134,8 @@ __global__ void __launch_bounds__(MT)
 k_mg_build1(const float4 *__restrict__ g, Dims4 d, Dims4 m, float4 *__restrict__ G,
             float4 *__restrict__ cpl, float4 *__restrict__ dinv, float wS, float wE, float lambda,
             const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (st->done == CG_EARLY) return;
   const int lim[4] = {d.x - 2, d.y - 2, d.z - 2, d.t - 2};  // last interior index
   const uint32_t n = (uint32_t)m.cells();
@@ -189,6 +191,8 @@ __global__ void __launch_bounds__(MT)
 k_mg_build(const float4 *__restrict__ Gp, const float4 *__restrict__ cp, Dims4 mp, Dims4 m,
            float4 *__restrict__ G, float4 *__restrict__ cpl, float4 *__restrict__ dinv,
            float lambda, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (st->done == CG_EARLY) return;
   const int ext[4] = {mp.x, mp.y, mp.z, mp.t};
   const uint32_t n = (uint32_t)m.cells();
@@ -242,6 +246,8 @@ k_mg_build(const float4 *__restrict__ Gp, const float4 *__restrict__ cp, Dims4 m
 __global__ void __launch_bounds__(MT)
 k_mg0_pre(const float4 *__restrict__ b, const float4 *__restrict__ g, float4 *__restrict__ x,
           Dims4 d, BoxDecoder bx, uint32_t nint, float c0, float omega, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
     int i, j, k, l;
@@ -267,61 +273,6 @@ __device__ __forceinline__ float4 a0_mul(const float4 *__restrict__ x, float4 gg
   return f4_axpy(-wS, nb, blk0_mul(gg, c0, xc));
 }
 
-// r = b - A x
-__global__ void __launch_bounds__(MT)
-k_mg0_resid(const float4 *__restrict__ b, const float4 *__restrict__ g,
-            const float4 *__restrict__ x, float4 *__restrict__ r, Dims4 d, BoxDecoder bx,
-            uint32_t nint, float c0, float wS, const CGState *st) {
-  if (mg_stop(st)) return;
-  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    r[id] = f4_sub(__ldg(b + id), a0_mul(x, __ldg(g + id), id, sY, sZ, sT, c0, wS));
-  }
-}
-
-// b1[K] = sum of r over the aggregate's interior cells
-__global__ void __launch_bounds__(MT)
-k_mg0_restrict(const float4 *__restrict__ r, float4 *__restrict__ b1, Dims4 d, Dims4 m,
-               const CGState *st) {
-  if (mg_stop(st)) return;
-  const int lim[4] = {d.x - 2, d.y - 2, d.z - 2, d.t - 2};
-  const uint32_t n = (uint32_t)m.cells();
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    int K[4];
-    uint32_t rest = q;
-    K[0] = rest % m.x; rest /= m.x;
-    K[1] = rest % m.y; rest /= m.y;
-    K[2] = rest % m.z; K[3] = rest / m.z;
-    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-    const int e0 = (2 + 2 * K[0] <= lim[0]), e1 = (2 + 2 * K[1] <= lim[1]);
-    const int e2 = (2 + 2 * K[2] <= lim[2]), e3 = (2 + 2 * K[3] <= lim[3]);
-    for (int dl = 0; dl <= e3; ++dl)
-      for (int dk = 0; dk <= e2; ++dk)
-        for (int dj = 0; dj <= e1; ++dj)
-          for (int di = 0; di <= e0; ++di)
-            s = f4_add(s, __ldg(r + d.index(1 + 2 * K[0] + di, 1 + 2 * K[1] + dj,
-                                             1 + 2 * K[2] + dk, 1 + 2 * K[3] + dl)));
-    b1[q] = s;
-  }
-}
-
-// x += e1[parent]
-__global__ void __launch_bounds__(MT)
-k_mg0_prolong(float4 *__restrict__ x, const float4 *__restrict__ e1, Dims4 d, BoxDecoder bx,
-              uint32_t nint, Dims4 m, const CGState *st) {
-  if (mg_stop(st)) return;
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    const float4 e = __ldg(e1 + m.index((i - 1) >> 1, (j - 1) >> 1, (k - 1) >> 1, (l - 1) >> 1));
-    x[id] = f4_add(x[id], e);
-  }
-}
-
 // x0 + e1[parent] at interior cell (i,j,k,l) of level 0.
 __device__ __forceinline__ float4 xp_at(const float4 *__restrict__ x, const float4 *__restrict__ e1,
                                         const Dims4 &d, const Dims4 &m, idx_t id, int i, int j,
@@ -330,41 +281,63 @@ __device__ __forceinline__ float4 xp_at(const float4 *__restrict__ x, const floa
                 __ldg(e1 + m.index((i - 1) >> 1, (j - 1) >> 1, (k - 1) >> 1, (l - 1) >> 1)));
 }
 
-// The level-0 post-smoothing with the prolongation folded in:
-// y = x + P e1 (formed on the fly at the cell and its neighbours; border
-// cells stay zero), z = y + omega D^-1 (b - A y); z . b for the PCG.
+// The same post-smoothing, one thread per interior (x, y, z) column walking
+// MG_TT consecutive t planes with y = x + P e1 at t-1, t, t+1 in registers
+// (the t neighbours cost no load).
+constexpr int MG_TT = 8;
 __global__ void __launch_bounds__(MT)
-k_mg0_post_prolong(const float4 *__restrict__ b, const float4 *__restrict__ g,
-                   const float4 *__restrict__ x, const float4 *__restrict__ e1,
-                   float4 *__restrict__ z, Dims4 d, BoxDecoder bx, uint32_t nint, Dims4 m,
-                   float c0, float wS, float omega, CGState *st, double *dpart, int init) {
+k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
+              const float4 *__restrict__ x, const float4 *__restrict__ e1, float4 *__restrict__ z,
+              Dims4 d, BoxDecoder bxyz, uint32_t nxyz, int tchunks, Dims4 m, float c0, float wS,
+              float omega, CGState *st, double *dpart, int init) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ double shd[MT / 32];
   __shared__ FF shff[MT / 32];
   FF dot = {0.f, 0.f};
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
-  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
-    int i, j, k, l;
-    bx.decode(n, i, j, k, l);
-    const idx_t id = d.index(i, j, k, l);
-    const float4 gg = __ldg(g + id), bb = __ldg(b + id);
-    const float4 yc = xp_at(x, e1, d, m, id, i, j, k, l);
-    float4 nb = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (l > 1) nb = f4_add(nb, xp_at(x, e1, d, m, id - sT, i, j, k, l - 1));
-    if (k > 1) nb = f4_add(nb, xp_at(x, e1, d, m, id - sZ, i, j, k - 1, l));
-    if (j > 1) nb = f4_add(nb, xp_at(x, e1, d, m, id - sY, i, j - 1, k, l));
-    if (i > 1) nb = f4_add(nb, xp_at(x, e1, d, m, id - 1, i - 1, j, k, l));
-    if (i < d.x - 2) nb = f4_add(nb, xp_at(x, e1, d, m, id + 1, i + 1, j, k, l));
-    if (j < d.y - 2) nb = f4_add(nb, xp_at(x, e1, d, m, id + sY, i, j + 1, k, l));
-    if (k < d.z - 2) nb = f4_add(nb, xp_at(x, e1, d, m, id + sZ, i, j, k + 1, l));
-    if (l < d.t - 2) nb = f4_add(nb, xp_at(x, e1, d, m, id + sT, i, j, k, l + 1));
-    const float4 res = f4_sub(bb, f4_axpy(-wS, nb, blk0_mul(gg, c0, yc)));
-    const float4 zz = f4_axpy(omega, blk0_solve(gg, c0, res), yc);
-    z[id] = zz;
-    ff_add(dot, zz.x * bb.x);
-    ff_add(dot, zz.y * bb.y);
-    ff_add(dot, zz.z * bb.z);
-    ff_add(dot, zz.w * bb.w);
+  const uint32_t n = nxyz * (uint32_t)tchunks;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const uint32_t cell = q % nxyz, tc = q / nxyz;
+    int i, j, k, unused;
+    bxyz.decode(cell, i, j, k, unused);
+    const int l0 = 1 + (int)tc * MG_TT;
+    const int l1 = min(l0 + MG_TT, d.t - 1);
+    idx_t id = d.index(i, j, k, l0);
+    // parents of the cell and of its x, y, z neighbours (t varies below)
+    const int pi = (i - 1) >> 1, pj = (j - 1) >> 1, pk = (k - 1) >> 1;
+    const int pim = (i - 2) >> 1, pip = i >> 1, pjm = (j - 2) >> 1, pjp = j >> 1;
+    const int pkm = (k - 2) >> 1, pkp = k >> 1;
+    const bool hxm = i > 1, hxp = i < d.x - 2, hym = j > 1, hyp = j < d.y - 2;
+    const bool hzm = k > 1, hzp = k < d.z - 2;
+    auto yat = [&](idx_t c, int a, int bb, int cc, int dd) {
+      return f4_add(__ldg(x + c), __ldg(e1 + m.index(a, bb, cc, dd)));
+    };
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ym = l0 > 1 ? yat(id - sT, pi, pj, pk, (l0 - 2) >> 1) : zero4;
+    float4 yc = yat(id, pi, pj, pk, (l0 - 1) >> 1);
+    for (int l = l0; l < l1; ++l, id += sT) {
+      const int pl = (l - 1) >> 1;
+      const float4 yp = l < d.t - 2 ? yat(id + sT, pi, pj, pk, l >> 1) : zero4;
+      float4 nb = f4_add(ym, yp);
+      if (hzm) nb = f4_add(nb, yat(id - sZ, pi, pj, pkm, pl));
+      if (hym) nb = f4_add(nb, yat(id - sY, pi, pjm, pk, pl));
+      if (hxm) nb = f4_add(nb, yat(id - 1, pim, pj, pk, pl));
+      if (hxp) nb = f4_add(nb, yat(id + 1, pip, pj, pk, pl));
+      if (hyp) nb = f4_add(nb, yat(id + sY, pi, pjp, pk, pl));
+      if (hzp) nb = f4_add(nb, yat(id + sZ, pi, pj, pkp, pl));
+      const float4 gg = __ldg(g + id), bb = __ldg(b + id);
+      const float4 res = f4_sub(bb, f4_axpy(-wS, nb, blk0_mul(gg, c0, yc)));
+      const float4 zz = f4_axpy(omega, blk0_solve(gg, c0, res), yc);
+      z[id] = zz;
+      ff_add(dot, zz.x * bb.x);
+      ff_add(dot, zz.y * bb.y);
+      ff_add(dot, zz.z * bb.z);
+      ff_add(dot, zz.w * bb.w);
+      ym = yc;
+      yc = yp;
+    }
   }
   const double bd = block_sum_ff<MT>(dot, shff);
   if (threadIdx.x == 0) dpart[blockIdx.x] = bd;
@@ -401,6 +374,8 @@ __global__ void __launch_bounds__(MT)
 k_mg0_resid_restrict(const float4 *__restrict__ b, const float4 *__restrict__ g,
                      const float4 *__restrict__ x, float4 *__restrict__ b1, Dims4 d, Dims4 m,
                      int nbx, float c0, float wS, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ float4 part[8][16];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -437,6 +412,8 @@ __global__ void __launch_bounds__(MT)
 k_mg0_post(const float4 *__restrict__ b, const float4 *__restrict__ g,
            const float4 *__restrict__ x, float4 *__restrict__ z, Dims4 d, BoxDecoder bx,
            uint32_t nint, float c0, float wS, float omega, CGState *st, double *dpart, int init) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ double shd[MT / 32];
   __shared__ FF shff[MT / 32];
@@ -521,6 +498,8 @@ __device__ __forceinline__ float4 dinv_mul(const float4 *__restrict__ dinv, idx_
 __global__ void __launch_bounds__(MT)
 k_mgc_pre(const float4 *__restrict__ b, const float4 *__restrict__ dinv, float4 *__restrict__ x,
           uint32_t n, float omega, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
     x[q] = f4_scale(omega, dinv_mul(dinv, q, __ldg(b + q)));
@@ -530,6 +509,8 @@ __global__ void __launch_bounds__(MT)
 k_mgc_resid(const float4 *__restrict__ b, const float4 *__restrict__ G,
             const float4 *__restrict__ cpl, const float4 *__restrict__ x, float4 *__restrict__ r,
             Dims4 m, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   const uint32_t n = (uint32_t)m.cells();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -542,6 +523,8 @@ k_mgc_resid(const float4 *__restrict__ b, const float4 *__restrict__ G,
 __global__ void __launch_bounds__(MT)
 k_mgc_restrict(const float4 *__restrict__ r, float4 *__restrict__ bn, Dims4 m, Dims4 mn,
                const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   const uint32_t n = (uint32_t)mn.cells();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -563,6 +546,8 @@ k_mgc_restrict(const float4 *__restrict__ r, float4 *__restrict__ bn, Dims4 m, D
 __global__ void __launch_bounds__(MT)
 k_mgc_prolong(float4 *__restrict__ x, const float4 *__restrict__ e, Dims4 m, Dims4 mn,
               const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   const uint32_t n = (uint32_t)m.cells();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -578,6 +563,8 @@ k_mgc_post(const float4 *__restrict__ b, const float4 *__restrict__ G,
            const float4 *__restrict__ cpl, const float4 *__restrict__ dinv,
            const float4 *__restrict__ x, float4 *__restrict__ xo, Dims4 m, float omega,
            const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   const uint32_t n = (uint32_t)m.cells();
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
@@ -595,6 +582,8 @@ __global__ void __launch_bounds__(MG_COARSEST)
 k_mgc_coarsest(const float4 *__restrict__ b, const float4 *__restrict__ G,
                const float4 *__restrict__ cpl, const float4 *__restrict__ dinv,
                float4 *__restrict__ xout, Dims4 m, float omega, int sweeps, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ float4 xs[2][MG_COARSEST];
   const int n = (int)m.cells();
@@ -650,6 +639,8 @@ __global__ void __launch_bounds__(MT)
 k_mgcg_update(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *__restrict__ p,
               const float4 *__restrict__ q, Dims4 d, BoxDecoder bx, uint32_t nint, CGState *st,
               float *fpart, int maxIter) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ float shf[MT / 32];
   const float a = st->alphaf;
@@ -692,6 +683,8 @@ k_mgcg_update_pre(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *
                   const float4 *__restrict__ q, const float4 *__restrict__ g,
                   float4 *__restrict__ x0, Dims4 d, BoxDecoder bx, uint32_t nint, float c0,
                   float omega, CGState *st, float *fpart, int maxIter) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   __shared__ float shf[MT / 32];
   const float a = st->alphaf;
@@ -732,6 +725,8 @@ k_mgcg_update_pre(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *
 __global__ void __launch_bounds__(MT)
 k_mgcg_direction(float4 *__restrict__ p, const float4 *__restrict__ z, Dims4 d, BoxDecoder bx,
                  uint32_t nint, const CGState *st, int init) {
+  pdl_wait();
+  pdl_launch_dependents();
   if (mg_stop(st)) return;
   const float b = st->betaf;
   for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
@@ -749,6 +744,8 @@ __global__ void __launch_bounds__(MT)
 k_mg_judge(const float4 *__restrict__ x, const float4 *__restrict__ b,
            const float4 *__restrict__ g, float4 *__restrict__ r, Dims4 d, BoxDecoder bx,
            uint32_t nint, float c0, float wS, float *fpart, unsigned int *counter, float *rmax) {
+  pdl_wait();
+  pdl_launch_dependents();
   __shared__ float shf[MT / 32];
   float mx = -FLT_MAX;
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
@@ -770,6 +767,29 @@ k_mg_judge(const float4 *__restrict__ x, const float4 *__restrict__ b,
       *rmax = m;
       *counter = 0;
     }
+  }
+}
+
+// Launches an MG kernel with programmatic stream serialisation: its blocks
+// are scheduled while the previous kernel drains and wait in pdl_wait until
+// that kernel's writes are visible.  Falls back to an ordinary launch if the
+// attribute is refused.
+template <typename... KArgs, typename... Args>
+void mg_launch(void (*k)(KArgs...), unsigned grid, unsigned block, cudaStream_t s,
+               Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k, args...) != cudaSuccess) {
+    cudaGetLastError();
+    k<<<grid, block, 0, s>>>(args...);
   }
 }
 
@@ -800,11 +820,11 @@ std::vector<Dims4> mg_level_dims(Dims4 d) {
 void launch_mg_build(const float4 *g, Dims4 d, const MGLevelPtrs *L, int nl, const OFConsts &c,
                      const MGParams &mp, const CGState *st, cudaStream_t s) {
   if (nl <= 0) return;
-  k_mg_build1<<<grid_for(L[0].m.cells(), MT, 8), MT, 0, s>>>(
-      g, d, L[0].m, L[0].G, L[0].cpl, L[0].dinv, c.wSmooth, c.wEnergy, mp.lambda, st);
+  mg_launch(k_mg_build1, grid_for(L[0].m.cells(), MT, 8), MT, s, g, d, L[0].m, L[0].G, L[0].cpl,
+            L[0].dinv, c.wSmooth, c.wEnergy, mp.lambda, st);
   for (int l = 1; l < nl; ++l)
-    k_mg_build<<<grid_for(L[l].m.cells(), MT, 8), MT, 0, s>>>(
-        L[l - 1].G, L[l - 1].cpl, L[l - 1].m, L[l].m, L[l].G, L[l].cpl, L[l].dinv, mp.lambda, st);
+    mg_launch(k_mg_build, grid_for(L[l].m.cells(), MT, 8), MT, s, L[l - 1].G, L[l - 1].cpl,
+              L[l - 1].m, L[l].m, L[l].G, L[l].cpl, L[l].dinv, mp.lambda, st);
 }
 
 void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0, float4 *z, Dims4 d,
@@ -816,46 +836,52 @@ void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0,
   const float c0 = c.diag, wS = c.wSmooth;
   int nl_ = 0;
   if (!pre_done) {
-    k_mg0_pre<<<nb0, MT, 0, s>>>(b0, g, x0, d, bx, nint, c0, mp.omega0, st);
+    mg_launch(k_mg0_pre, nb0, MT, s, b0, g, x0, d, bx, nint, c0, mp.omega0, st);
     ++nl_;
   }
   if (nl == 0) {
-    k_mg0_post<<<nb0, MT, 0, s>>>(b0, g, x0, z, d, bx, nint, c0, wS, mp.omega0, st, dpart, init);
+    mg_launch(k_mg0_post, nb0, MT, s, b0, g, x0, z, d, bx, nint, c0, wS, mp.omega0, st, dpart,
+              init);
     if (launches) *launches += nl_;  // the caller counts one
     return;
   }
   {
     const int nbx = (d.x - 2 + 31) / 32;
     const long long nblk = (long long)nbx * L[0].m.y * L[0].m.z * L[0].m.t;
-    k_mg0_resid_restrict<<<(unsigned)nblk, MT, 0, s>>>(b0, g, x0, L[0].b, d, L[0].m, nbx, c0, wS,
-                                                      st);
+    mg_launch(k_mg0_resid_restrict, (unsigned)nblk, MT, s, b0, g, x0, L[0].b, d, L[0].m, nbx, c0,
+              wS, st);
     ++nl_;
   }
   for (int l = 0; l + 1 < nl; ++l) {
     const uint32_t n = (uint32_t)L[l].m.cells();
     const int nb = grid_for(n, MT, 8);
-    k_mgc_pre<<<nb, MT, 0, s>>>(L[l].b, L[l].dinv, L[l].x, n, mp.omegac, st);
-    k_mgc_resid<<<nb, MT, 0, s>>>(L[l].b, L[l].G, L[l].cpl, L[l].x, L[l].r, L[l].m, st);
-    k_mgc_restrict<<<grid_for(L[l + 1].m.cells(), MT, 8), MT, 0, s>>>(L[l].r, L[l + 1].b, L[l].m,
-                                                                      L[l + 1].m, st);
+    mg_launch(k_mgc_pre, nb, MT, s, L[l].b, L[l].dinv, L[l].x, n, mp.omegac, st);
+    mg_launch(k_mgc_resid, nb, MT, s, L[l].b, L[l].G, L[l].cpl, L[l].x, L[l].r, L[l].m, st);
+    mg_launch(k_mgc_restrict, grid_for(L[l + 1].m.cells(), MT, 8), MT, s, L[l].r, L[l + 1].b,
+              L[l].m, L[l + 1].m, st);
     nl_ += 3;
   }
   const MGLevelPtrs &B = L[nl - 1];
-  k_mgc_coarsest<<<1, MG_COARSEST, 0, s>>>(B.b, B.G, B.cpl, B.dinv, B.x, B.m, mp.omegac,
-                                           mp.coarse_sweeps, st);
+  mg_launch(k_mgc_coarsest, 1, MG_COARSEST, s, B.b, B.G, B.cpl, B.dinv, B.x, B.m, mp.omegac,
+            mp.coarse_sweeps, st);
   ++nl_;
   for (int l = nl - 2; l >= 0; --l) {
     const uint32_t n = (uint32_t)L[l].m.cells();
     const int nb = grid_for(n, MT, 8);
-    k_mgc_prolong<<<nb, MT, 0, s>>>(L[l].x, L[l + 1].x, L[l].m, L[l + 1].m, st);
-    k_mgc_post<<<nb, MT, 0, s>>>(L[l].b, L[l].G, L[l].cpl, L[l].dinv, L[l].x, L[l].r, L[l].m,
-                                 mp.omegac, st);
+    mg_launch(k_mgc_prolong, nb, MT, s, L[l].x, L[l + 1].x, L[l].m, L[l + 1].m, st);
+    mg_launch(k_mgc_post, nb, MT, s, L[l].b, L[l].G, L[l].cpl, L[l].dinv, L[l].x, L[l].r, L[l].m,
+              mp.omegac, st);
     // the post-smoothed iterate is in r; it becomes this level's x
     std::swap(L[l].x, L[l].r);
     nl_ += 2;
   }
-  k_mg0_post_prolong<<<nb0, MT, 0, s>>>(b0, g, x0, L[0].x, z, d, bx, nint, L[0].m, c0, wS,
-                                        mp.omega0, st, dpart, init);
+  {
+    const BoxDecoder bxyz = make_decoder(d.x - 2, d.y - 2, d.z - 2, 1, 1, 1, 0);
+    const uint32_t nxyz = (uint32_t)((long long)(d.x - 2) * (d.y - 2) * (d.z - 2));
+    const int tchunks = (d.t - 2 + MG_TT - 1) / MG_TT;
+    mg_launch(k_mg0_post_tw, grid_for((long long)nxyz * tchunks, MT, 8), MT, s, b0, g, x0, L[0].x,
+              z, d, bxyz, nxyz, tchunks, L[0].m, c0, wS, mp.omega0, st, dpart, init);
+  }
   ++nl_;
   if (launches) *launches += nl_ - 1;  // the caller counts one
 }
@@ -863,31 +889,110 @@ void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0,
 void launch_mgcg_update(float4 *x, float4 *r, const float4 *p, const float4 *q, Dims4 d,
                         CGState *st, float *fpart, int maxIter, cudaStream_t s) {
   const uint32_t nint = interior_n(d);
-  k_mgcg_update<<<grid_for(nint > 0 ? nint : 1, MT, 8), MT, 0, s>>>(x, r, p, q, d, interior_box(d),
-                                                                  nint, st, fpart, maxIter);
+  mg_launch(k_mgcg_update, grid_for(nint > 0 ? nint : 1, MT, 8), MT, s, x, r, p, q, d,
+            interior_box(d), nint, st, fpart, maxIter);
 }
 void launch_mgcg_update_pre(float4 *x, float4 *r, const float4 *p, const float4 *q,
                             const float4 *g, float4 *x0, Dims4 d, const OFConsts &c,
                             const MGParams &mp, CGState *st, float *fpart, int maxIter,
                             cudaStream_t s) {
   const uint32_t nint = interior_n(d);
-  k_mgcg_update_pre<<<grid_for(nint > 0 ? nint : 1, MT, 8), MT, 0, s>>>(
-      x, r, p, q, g, x0, d, interior_box(d), nint, c.diag, mp.omega0, st, fpart, maxIter);
+  mg_launch(k_mgcg_update_pre, grid_for(nint > 0 ? nint : 1, MT, 8), MT, s, x, r, p, q, g, x0, d,
+            interior_box(d), nint, c.diag, mp.omega0, st, fpart, maxIter);
 }
 
 void launch_mg_judge(const float4 *x, const float4 *b, const float4 *g, float4 *r, Dims4 d,
                      const OFConsts &c, float *fpart, unsigned int *counter, float *rmax,
                      cudaStream_t s) {
   const uint32_t nint = interior_n(d);
-  k_mg_judge<<<grid_for(nint > 0 ? nint : 1, MT, 8), MT, 0, s>>>(
-      x, b, g, r, d, interior_box(d), nint, c.diag, c.wSmooth, fpart, counter, rmax);
+  mg_launch(k_mg_judge, grid_for(nint > 0 ? nint : 1, MT, 8), MT, s, x, b, g, r, d, interior_box(d),
+            nint, c.diag, c.wSmooth, fpart, counter, rmax);
 }
 
 void launch_mgcg_direction(float4 *p, const float4 *z, Dims4 d, const CGState *st, int init,
                            cudaStream_t s) {
   const uint32_t nint = interior_n(d);
-  k_mgcg_direction<<<grid_for(nint > 0 ? nint : 1, MT, 8), MT, 0, s>>>(p, z, d, interior_box(d),
-                                                                     nint, st, init);
+  mg_launch(k_mgcg_direction, grid_for(nint > 0 ? nint : 1, MT, 8), MT, s, p, z, d, interior_box(d),
+            nint, st, init);
+}
+
+// ---------------------------------------------------------------------------
+// Separable extrapolation sweep (blurType 2): knCvExpolBlur4d
+// (optflow4d.cpp:613-626) sets every unmarked interior cell to 1/81 of the
+// sum over its 3^4 neighbourhood of the source.  That sum is formed here in
+// two streaming passes, equal to the reference's 81-term sum up to rounding:
+//   S2(x,y,z,t) = the 3x3 (x,y) box sum of the source, for interior x, y and
+//                 every z, t;
+//   out         = 1/81 of the 3x3 (z,t) box sum of S2, each thread walking
+//                 t with the z sums of t-1, t, t+1 in registers.
+// Marked and border cells are not written: both sweep buffers hold their
+// values.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(MT)
+k_sep_xy(const float4 *__restrict__ src, float4 *__restrict__ s2, Dims4 d, BoxDecoder bx,
+         uint32_t n) {
+  const idx_t sY = d.x;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(q, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const idx_t r = id + dy * sY;
+      s = f4_add(s, f4_add(f4_add(__ldg(src + r - 1), __ldg(src + r)), __ldg(src + r + 1)));
+    }
+    s2[id] = s;
+  }
+}
+
+constexpr int SEP_TT = 8;  // t planes per work item of the z-t pass
+
+__global__ void __launch_bounds__(MT)
+k_sep_zt(const float4 *__restrict__ s2, const float *__restrict__ mark, float4 *__restrict__ out,
+         Dims4 d, BoxDecoder bx, uint32_t nxyz, int tchunks) {
+  const idx_t sZ = d.sz(), sT = d.st();
+  const uint32_t n = nxyz * (uint32_t)tchunks;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const uint32_t cell = q % nxyz, tc = q / nxyz;
+    int i, j, k, unused;
+    bx.decode(cell, i, j, k, unused);
+    const int l0 = 1 + (int)tc * SEP_TT;
+    const int l1 = min(l0 + SEP_TT, d.t - 1);
+    idx_t id = d.index(i, j, k, l0);
+    auto zsum = [&](idx_t c) {
+      return f4_add(f4_add(__ldg(s2 + c - sZ), __ldg(s2 + c)), __ldg(s2 + c + sZ));
+    };
+    float4 zm = zsum(id - sT), zc = zsum(id);
+    for (int l = l0; l < l1; ++l, id += sT) {
+      const float4 zp = zsum(id + sT);
+      if (__ldg(mark + id) == 0.f) {
+        const float4 v = f4_add(f4_add(zm, zc), zp);
+        out[id] = make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
+      }
+      zm = zc;
+      zc = zp;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_expol_sep(const float4 *in, float4 *out, float4 *s2, const float *mark, Dims4 d,
+                      cudaStream_t s) {
+  if (d.x < 3 || d.y < 3 || d.z < 3 || d.t < 3) return;
+  // S2 over interior x, y and every z, t
+  const BoxDecoder bxy = make_decoder(d.x - 2, d.y - 2, d.z, 1, 1, 0, 0);
+  const uint32_t nxy = (uint32_t)((long long)(d.x - 2) * (d.y - 2) * d.z * d.t);
+  k_sep_xy<<<grid_for(nxy, MT, 8), MT, 0, s>>>(in, s2, d, bxy, nxy);
+  // z-t sums over interior cells
+  const BoxDecoder bxyz = make_decoder(d.x - 2, d.y - 2, d.z - 2, 1, 1, 1, 0);
+  const uint32_t nxyz = (uint32_t)((long long)(d.x - 2) * (d.y - 2) * (d.z - 2));
+  const int tchunks = (d.t - 2 + SEP_TT - 1) / SEP_TT;
+  k_sep_zt<<<grid_for((long long)nxyz * tchunks, MT, 8), MT, 0, s>>>(s2, mark, out, d, bxyz, nxyz,
+                                                                     tchunks);
 }
 
 }  // namespace flof

@@ -54,9 +54,6 @@ struct TG {
 // planes share every slab (24 slabs per 8 output planes), four in flight.
 template <int S> using BlurGeom = TG<S, 4, 8, 1, 1, 2>;
 using ExpolGeom = TG<1, 8, 2, 4, 2, 4, 3>;
-// The separable sweep: the same tiles (and keep-mask layout), two blocks per
-// SM so that its box sums and accumulators fit in registers.
-using ExpolSepGeom = TG<1, 8, 2, 4, 2, 4, 2>;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -186,7 +183,7 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   const int tile = blockIdx.x;
   // this block's tile in the zero-tracking flags
   auto self = [] { return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x; };
-  if (MODE >= 1 && nz_in) {
+  if (MODE == 1 && nz_in) {
     const int ntile_xy = gridDim.x, tiles_y = ntile_xy / tiles_x;
     // Skip when the input is zero over the tile and its 1-cell halo, and the
     // tile is zero in the output: the sweep would write +0 over +0.  The halo
@@ -224,7 +221,7 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   // MODE 1: bit (oz*DT + o)*RY + q set = cell (x, y0+RY*ty+q, z0+oz, t0+o)
   // keeps its value (loaded now, used after the slab walk)
   unsigned keep = 0xffffu;
-  if (MODE >= 1) {
+  if (MODE == 1) {
     const int ygroups = (d.y + RY - 1) / RY, zgroups = (d.z + DZ - 1) / DZ;
     const int yg = y0 / RY + ty;
     if (x < d.x && yg < ygroups)
@@ -279,39 +276,6 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       return;
     }
     const V4 *cur = (const V4 *)(raw + (p % NS) * G::STRIDE);
-    if constexpr (MODE == 2) {
-      // separable: the slab's 3x3 (x,y) box sums of the thread's RY output
-      // rows (x sums of each row, then y sums), added once to every output
-      // plane this slab feeds
-      static_assert(S == 1, "the separable sweep is the 3^4 box");
-      V4 xs[RY + 2];
-#pragma unroll
-      for (int k = 0; k < RY + 2; ++k) {
-        const V4 *row = cur + (RY * ty + k) * G::W + tx;
-        xs[k] = row[0];
-        acc4(xs[k], row[1]);
-        acc4(xs[k], row[2]);
-      }
-#pragma unroll
-      for (int q = 0; q < RY; ++q) {
-        V4 s2 = xs[q];
-        acc4(s2, xs[q + 1]);
-        acc4(s2, xs[q + 2]);
-#pragma unroll
-        for (int oz = 0; oz < DZ; ++oz) {
-          const int zk = zk0 - oz;
-          if (zk < -1 || zk > 1) continue;
-#pragma unroll
-          for (int o = 0; o < DT; ++o) {
-            const int vt = vt0 - o;
-            if (vt < -1 || vt > 1) continue;
-            acc4(val[oz][o][q], s2);
-          }
-        }
-      }
-      __syncthreads();
-      continue;
-    }
     // slab rows RY*ty .. RY*ty+RY-1+2S feed output rows RY*ty+q via yj = k-q-S
 #pragma unroll
     for (int k = 0; k < RY + 2 * S; ++k) {
@@ -366,7 +330,7 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
 
   if (x >= d.x) return;
-  uint32_t fbits = 0;  // MODE 1, 2: face bits of the nonzero values this thread writes
+  uint32_t fbits = 0;  // MODE 1: face bits of the nonzero values this thread writes
   constexpr int P1 = (S + 1) * (S + 1);
 #pragma unroll
   for (int oz = 0; oz < DZ; ++oz) {
@@ -406,7 +370,7 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       }
     }
   }
-  if (MODE >= 1 && nz_in) {
+  if (MODE == 1 && nz_in) {
     // threads past the grid's end returned above; one atomic per warp
     const unsigned act = __activemask();
     const uint32_t w = __reduce_or_sync(act, fbits);
@@ -569,10 +533,7 @@ void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uin
 
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
                       uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
-                      cudaStream_t st, bool separable) {
-  if (separable)
-    return launch_tma<1, 2, ExpolSepGeom>(in, out, d, nullptr, mask, nullptr, 0, err, st, nz_in,
-                                          nz_out, keep_nz);
+                      cudaStream_t st) {
   return launch_tma<1, 1, ExpolGeom>(in, out, d, nullptr, mask, nullptr, 0, err, st, nz_in,
                                      nz_out, keep_nz);
 }
