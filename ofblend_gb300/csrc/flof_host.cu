@@ -609,8 +609,9 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       CK(cudaMemcpyAsync(B, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
       if (blurType != FLOF_BLUR_GAUSS_SEPARABLE) {  // the separable sweep reads the marker
         CK(cudaMemsetAsync(tflags.p, 0, 3 * ntiles * sizeof(uint32_t), c->stream));
-        KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 20,
-            launch_expol_mask(marker.f(), A, (uint16_t *)mask.p, fA, fB, fKeep, d, c->stream));
+        KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 4,
+            launch_expol_mask(marker.f(), A, (uint16_t *)mask.p, nullptr, nullptr, nullptr, d,
+                              c->stream));
       }
     }
     for (int s = 0; s < doCvExtrapol; ++s) {
@@ -623,8 +624,7 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       }
       bool tma = false;
       KLP(c, KC_EXPOL, d.x, d.cells() * 32,
-          tma = launch_expol_tma(A, B, (const uint16_t *)mask.p, track ? fA : nullptr,
-                                 track ? fB : nullptr, fKeep, d, c->dev_err, c->stream));
+          tma = launch_expol_tw(A, B, (const uint16_t *)mask.p, d, c->dev_err, c->stream));
       if (!tma) {
         // the flags no longer describe the buffers once a sweep runs untracked
         track = false;

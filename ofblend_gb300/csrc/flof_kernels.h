@@ -302,6 +302,10 @@ size_t expol_tiles(Dims4 d);
 // first.  Flag pointers may be null (no zero tracking).
 void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
                        uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st);
+// The sweep walking t with three output planes' sums in registers (the
+// same per-cell order and results); false when TMA is unavailable.
+bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                     cudaStream_t st);
 // nz_in / nz_out: the flags of the in and out buffers (null: no skipping).
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
                       uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,

@@ -378,6 +378,144 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
 }
 
+// The extrapolation sweep walking t.  A block owns a 32 x 16 (x,y) tile
+// and ETW_DZ consecutive z planes and walks ETW_TC + 2 t planes; for each
+// t plane it takes the ETW_DZ + 2 (x,y) slabs (with their one-cell halo)
+// that its outputs need, in z order, one TMA copy each, ETW_NS in flight.
+// Each thread keeps the running sums of its cells for three output planes
+// in registers: slab plane tt adds the taps vt = +1 of output tt - 1 (which
+// is then complete and written), vt = 0 of output tt and vt = -1 of output
+// tt + 1 (which starts there).  Every output thus adds its 81 taps in the
+// reference's order (t, z, y, x) with float adds in sequence, and the loop
+// body is the same for every plane: no run-time choice of outputs.
+constexpr int ETW_NW = 8, ETW_RY = 2, ETW_DZ = 2, ETW_TC = 8, ETW_NS = 4;
+constexpr int ETW_TY = ETW_NW * ETW_RY;
+constexpr int ETW_W = TX + 2, ETW_H = ETW_TY + 2;
+constexpr int ETW_BYTES = ETW_W * ETW_H * 16;
+constexpr int ETW_STRIDE = (ETW_BYTES + 127) / 128 * 128;
+constexpr int ETW_SMEM = ETW_NS * ETW_STRIDE;
+constexpr int ETW_KZ = ETW_DZ + 2;  // slabs per t plane
+static_assert(ETW_RY == ExpolGeom::RY && ETW_DZ == ExpolGeom::DZ,
+              "the keep mask groups rows and z planes as the sweep does");
+
+__global__ void __launch_bounds__(32 * ETW_NW, 3)
+k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
+           int tiles_x, const uint16_t *__restrict__ fixed, int *err) {
+  extern __shared__ __align__(128) unsigned char raw[];
+  __shared__ __align__(8) uint64_t bar[ETW_NS];
+  constexpr int RY = ETW_RY, DZ = ETW_DZ, KZ = ETW_KZ, NS = ETW_NS;
+  constexpr int DT = ExpolGeom::DT;  // t planes per keep-mask word
+  const int tile = blockIdx.x;
+  const int x0 = (tile % tiles_x) * TX, y0 = (tile / tiles_x) * ETW_TY;
+  const int z0 = blockIdx.y * DZ, t0 = blockIdx.z * ETW_TC;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x = x0 + tx;
+  const int ygroups = (d.y + RY - 1) / RY, zgroups = (d.z + DZ - 1) / DZ;
+  const int yg = y0 / RY + ty;
+  const bool xy_ok = x < d.x && yg < ygroups;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int b = 0; b < NS; ++b) mbar_init(&bar[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  const int NP = (ETW_TC + 2) * KZ;  // slab p: plane t0 - 1 + p / KZ, z0 - 1 + p % KZ
+  auto issue = [&](int p) {
+    uint64_t *b = &bar[p % NS];
+    mbar_expect_tx(b, ETW_BYTES);
+    tma_load_slab(raw + (p % NS) * ETW_STRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + p % KZ,
+                  t0 - 1 + p / KZ, b);
+  };
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int p = 0; p < NS - 1; ++p) issue(p);
+  }
+  // running sums of outputs tt - 1 (A), tt (B) and tt + 1 (C)
+  P4 A[DZ][RY], B[DZ][RY], C[DZ][RY];
+#pragma unroll
+  for (int oz = 0; oz < DZ; ++oz)
+#pragma unroll
+    for (int q = 0; q < RY; ++q) {
+      memset(&A[oz][q], 0, sizeof(P4));
+      memset(&B[oz][q], 0, sizeof(P4));
+    }
+  for (int j = 0; j < ETW_TC + 2; ++j) {
+#pragma unroll
+    for (int oz = 0; oz < DZ; ++oz)
+#pragma unroll
+      for (int q = 0; q < RY; ++q) memset(&C[oz][q], 0, sizeof(P4));
+#pragma unroll
+    for (int zk = 0; zk < KZ; ++zk) {
+      const int p = j * KZ + zk;
+      // buffer (p - 1) % NS was released by the barrier that ended slab p - 1
+      if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
+      const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
+          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
+        }
+        __syncthreads();
+        return;
+      }
+      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE);
+#pragma unroll
+      for (int k = 0; k < RY + 2; ++k) {
+        const P4 *row = cur + (RY * ty + k) * ETW_W + tx;
+        const P4 a0 = row[0], a1 = row[1], a2 = row[2];
+#pragma unroll
+        for (int oz = 0; oz < DZ; ++oz) {
+          const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
+          if (zrel < -1 || zrel > 1) continue;
+#pragma unroll
+          for (int q = 0; q < RY; ++q) {
+            const int yj = k - q - 1;
+            if (yj < -1 || yj > 1) continue;
+            // vt = -1 of output tt + 1, vt = 0 of output tt, vt = +1 of output tt - 1
+            acc4(C[oz][q], a0);
+            acc4(C[oz][q], a1);
+            acc4(C[oz][q], a2);
+            acc4(B[oz][q], a0);
+            acc4(B[oz][q], a1);
+            acc4(B[oz][q], a2);
+            acc4(A[oz][q], a0);
+            acc4(A[oz][q], a1);
+            acc4(A[oz][q], a2);
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // output tt - 1 = t0 - 2 + j is complete
+    const int t = t0 - 2 + j;
+    if (j >= 2 && xy_ok && t < d.t) {
+      const unsigned keep =
+          __ldg(fixed + (((size_t)(t / DT) * zgroups + blockIdx.y) * ygroups + yg) * d.x + x);
+#pragma unroll
+      for (int oz = 0; oz < DZ; ++oz) {
+        const int z = z0 + oz;
+        if (z >= d.z) break;
+#pragma unroll
+        for (int q = 0; q < RY; ++q) {
+          const int y = y0 + RY * ty + q;
+          if (y >= d.y) continue;
+          if (keep >> ((oz * DT + t % DT) * RY + q) & 1u) continue;
+          const float4 v = unpack4(A[oz][q]);
+          dst[d.index(x, y, z, t)] =
+              make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
+        }
+      }
+    }
+#pragma unroll
+    for (int oz = 0; oz < DZ; ++oz)
+#pragma unroll
+      for (int q = 0; q < RY; ++q) {
+        A[oz][q] = B[oz][q];
+        B[oz][q] = C[oz][q];
+      }
+  }
+}
+
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -529,6 +667,27 @@ void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uin
   const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + ExpolGeom::TY - 1) / ExpolGeom::TY;
   k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, src, mask, nz_a, nz_b, keep_nz, d,
                                                  ygroups, zgroups, tiles_x, tiles_y, n);
+}
+
+bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                     cudaStream_t st) {
+  const int zgroups = (d.z + ETW_DZ - 1) / ETW_DZ, tgroups = (d.t + ETW_TC - 1) / ETW_TC;
+  if (zgroups > 65535 || tgroups > 65535) return false;
+  CUtensorMap map;
+  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H)) return false;
+  static const bool attr = [] {
+    if (cudaFuncSetAttribute(k_expol_tw, cudaFuncAttributeMaxDynamicSharedMemorySize, ETW_SMEM) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  }();
+  if (!attr) return false;
+  const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + ETW_TY - 1) / ETW_TY;
+  dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
+  k_expol_tw<<<grid, 32 * ETW_NW, ETW_SMEM, st>>>(map, out, d, tiles_x, mask, err);
+  return true;
 }
 
 bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
