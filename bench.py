@@ -52,6 +52,8 @@ def args_():
     ap.add_argument("--blur-type", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-oracle64", action="store_true",
+                    help="--workload mixed: skip the FP64 oracle solve (minutes on the host)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-mode record of the default line")
     ap.add_argument("--train-pairs", type=int, default=256)
@@ -571,9 +573,28 @@ def run_gpu(a):
     sink = {"v01": pin(W.v01.shape), "v10": pin(W.v10.shape),
             "out4": [pin(W.out4.shape) for _ in ALPHAS],
             "frame": [pin(W.dst.shape) for _ in range(NFRAMEBUF)]}
+    def copy_rates():
+        """GB/s of one hi-res input up and back down on the copy stream."""
+        g = W.g_hi0
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        tc = time.perf_counter()
+        g.upload_async(pinned["hi0"])
+        g.copy_wait()
+        ctx.synchronize()
+        up = time.perf_counter() - tc
+        tc = time.perf_counter()
+        g.download_async(pinned["hi0"])
+        g.copy_wait()
+        ctx.synchronize()
+        down = time.perf_counter() - tc
+        nb = pinned["hi0"].nbytes
+        return round(nb / up / 1e9, 1), round(nb / down / 1e9, 1)
+
     e2e_val = None
     e2e_extra = {}
     if a.e2e_steps > 0:
+        rates_before = copy_rates()
         W.step_e2e(pinned, sink, ctx)
         torch.cuda.synchronize()
         barrier(world)
@@ -586,24 +607,12 @@ def run_gpu(a):
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0, world)
         e2e_val = round(job_rate(2 * a.e2e_steps, world, e2e_s), 4)
-        # the copy rates the transfers run at (one hi-res input up, the
-        # frames' bytes down, on the context's copy stream)
-        g = W.g_hi0
-        ctx.synchronize()
-        tc = time.perf_counter()
-        g.upload_async(pinned["hi0"])
-        g.copy_wait()
-        ctx.synchronize()
-        up = time.perf_counter() - tc
-        tc = time.perf_counter()
-        g.download_async(pinned["hi0"])
-        g.copy_wait()
-        ctx.synchronize()
-        down = time.perf_counter() - tc
+        # the copy rates the transfers run at, before and after the e2e steps
+        rates_after = copy_rates()
         e2e_extra = {"ms_per_step": round(e2e_s * 1e3 / a.e2e_steps, 3),
                      "ms_per_step_min": round(min(per) * 1e3, 3),
-                     "h2d_GBps": round(pinned["hi0"].nbytes / up / 1e9, 1),
-                     "d2h_GBps": round(pinned["hi0"].nbytes / down / 1e9, 1)}
+                     "h2d_GBps": rates_after[0], "d2h_GBps": rates_after[1],
+                     "h2d_d2h_GBps_before": list(rates_before)}
 
     st = list(W.stats)
     iters = [s["solves"] for s in st]
@@ -804,8 +813,10 @@ def run_batch(a):
 
 def run_mixed(a):
     """Mixed precision (BF16 gradient, FP64 residuals, iterative refinement)
-    against the FP32 solve at 96^4 with two drops per data set.  The errors
-    against the FP64 oracle are measured by tests/test_gpu_batch.py."""
+    against the FP32 solve at 96^4 with two drops per data set, and the FP32
+    solve of the inputs rounded to BF16 (the SDFs stored in BF16).  Each
+    deformation, and the SDF it deforms at alpha 0.5, is compared with the
+    FP64 CPU oracle's solve of the same inputs."""
     import torch
     import ofblend_gb300 as F
     from ofblend_gb300 import synth
@@ -840,6 +851,40 @@ def run_mixed(a):
         res[prec] = {"s": min(times), "vel": v.to_numpy(), "stats": st}
     d96 = float(np.linalg.norm(res["mixed"]["vel"] - res["fp32"]["vel"]) /
                 np.linalg.norm(res["fp32"]["vel"]))
+    # The SDF inputs stored in BF16: the same FP32 solve on inputs rounded to
+    # BF16 (round to nearest even), to measure what the data term makes of it.
+    h0, h1 = g0.to_numpy(), g1.to_numpy()
+
+    def bf16(x):
+        u = x.view(np.uint32).astype(np.uint64)
+        u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+        return u.astype(np.uint32).view(np.float32)
+    b0 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(bf16(h0))
+    b1 = F.Grid4Real(dims=dims, ctx=ctx).from_numpy(bf16(h1))
+    v.setConst(0.0)
+    F.opticalFlowMultiscale4d(v, b0, b1, **p)
+    res["bf16_sdf"] = {"vel": v.to_numpy()}
+    del b0, b1
+    errors = None
+    if not a.no_oracle64:
+        # the FP64 CPU oracle (the reference's -DDOUBLEPRECISION build restated)
+        # on the same inputs; deformed SDFs at alpha 0.5 in cells
+        import oracle
+        o64, o32 = oracle.get(True), oracle.get(False)
+        t0 = time.perf_counter()
+        ref, _, _ = o64.opticalFlowMultiscale4d(np.zeros(h0.shape + (4,), np.float64),
+                                                h0.astype(np.float64), h1.astype(np.float64),
+                                                **{k: v_ for k, v_ in p.items() if k != "blurType"})
+        t64 = time.perf_counter() - t0
+        sdf0 = synth.sdf4d(s0, dims)
+        ref_sdf = o64.advect4d(ref, sdf0.astype(np.float64), 0.5)
+        errors = {"oracle_fp64_seconds": round(t64, 1)}
+        for key in ("fp32", "mixed", "bf16_sdf"):
+            x = res[key]["vel"]
+            errors[key] = {
+                "rel_l2_vs_fp64": float(np.linalg.norm(x.astype(np.float64) - ref) / np.linalg.norm(ref)),
+                "sdf_cells_vs_fp64": float(np.abs(o32.advect4d(x, sdf0, 0.5).astype(np.float64)
+                                                  - ref_sdf).max())}
 
     m = res["mixed"]["stats"]
     line = {
@@ -855,6 +900,7 @@ def run_mixed(a):
         "mixed_cg_iterations": m["cg_total_iterations"],
         "mixed_true_residual_finest": m["true_residual"][-1] if m["true_residual"] else None,
         "mixed_vs_fp32_rel_l2_96": d96,
+        "errors_vs_fp64_oracle": errors,
     }
     print(json.dumps(line), flush=True)
     ctx.close()

@@ -587,8 +587,6 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
     fail(FLOF_E_ARG, "postVelBlur must be finite");
   DBuf marker(c, real_bytes(d)), tmp(c, vec_bytes(d));
   DBuf mask(c, expol_mask_words(d) * sizeof(uint16_t));
-  const size_t ntiles = expol_tiles(d);
-  DBuf tflags(c, 3 * ntiles * sizeof(uint32_t));  // zero tracking: buffer A, buffer B, kept
   DBuf s2;  // the separable sweep's (x,y) box sums (blurType 2)
   int singleStep = 0;
   if (postVelBlur < blurThreshold) singleStep = 1;
@@ -601,18 +599,13 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
     KLP(c, KC_PROJECT, d.x, d.cells() * 44,
         launch_project_cells(dst, vel, phiOrg, phiTarget, marker.f(), d, threshPhi, maxIter,
                                c->stream));
-    uint32_t *fA = (uint32_t *)tflags.p, *fB = fA + ntiles, *fKeep = fB + ntiles;
-    bool track = true;
     if (doCvExtrapol > 0) {
       // The sweeps only rewrite unmarked interior cells; both buffers carry
       // the projected values everywhere else (the reference's tmp copy).
       CK(cudaMemcpyAsync(B, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
-      if (blurType != FLOF_BLUR_GAUSS_SEPARABLE) {  // the separable sweep reads the marker
-        CK(cudaMemsetAsync(tflags.p, 0, 3 * ntiles * sizeof(uint32_t), c->stream));
+      if (blurType != FLOF_BLUR_GAUSS_SEPARABLE)  // the separable sweep reads the marker
         KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 4,
-            launch_expol_mask(marker.f(), A, (uint16_t *)mask.p, nullptr, nullptr, nullptr, d,
-                              c->stream));
-      }
+            launch_expol_mask(marker.f(), (uint16_t *)mask.p, d, c->stream));
     }
     for (int s = 0; s < doCvExtrapol; ++s) {
       if (blurType == FLOF_BLUR_GAUSS_SEPARABLE) {
@@ -625,17 +618,9 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       bool tma = false;
       KLP(c, KC_EXPOL, d.x, d.cells() * 32,
           tma = launch_expol_tw(A, B, (const uint16_t *)mask.p, d, c->dev_err, c->stream));
-      if (!tma) {
-        // the flags no longer describe the buffers once a sweep runs untracked
-        track = false;
+      if (!tma)
         KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_slab(A, B, marker.f(), d, c->stream));
-      }
-      float4 *sw = A;
-      A = B;
-      B = sw;
-      uint32_t *fs = fA;
-      fA = fB;
-      fB = fs;
+      std::swap(A, B);
     }
     if (postVelBlur > 1e-6f) gauss_blur(c, (float *)A, d, 4, (float)(0.5 * postVelBlur), blurType);
     const int resetBnd = trunc_f(resetBndWidth * (float)d.x) + 1;

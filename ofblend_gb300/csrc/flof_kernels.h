@@ -290,26 +290,12 @@ bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const floa
 // Which cells those are comes from a packed mask that launch_expol_mask
 // builds from the marker once per round: expol_mask_words(d) 16-bit words.
 size_t expol_mask_words(Dims4 d);
-// Zero tracking of the sweeps.  A sweep block owns one tile of cells; a tile
-// whose input neighbourhood is all zero computes +0 everywhere (sums that
-// start at +0 never give -0), so when its destination tile is already zero
-// the block has nothing to write and returns at once.  Flags per tile, 0 or
-// 1: nz_a / nz_b = some cell of the tile is nonzero in that buffer, keep_nz =
-// some cell the sweep leaves alone is nonzero.  expol_tiles(d) tiles each.
-size_t expol_tiles(Dims4 d);
-// Builds the keep-mask from the marker and the three flag arrays from the
-// projected field src (both sweep buffers hold it); the flags must be zeroed
-// first.  Flag pointers may be null (no zero tracking).
-void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
-                       uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st);
-// The sweep walking t with three output planes' sums in registers (the
-// same per-cell order and results); false when TMA is unavailable.
+void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st);
+// The sweep walking t with three output planes' running sums in registers
+// (every output adds its 81 taps in the reference's order); false when TMA
+// is unavailable (the caller then uses launch_expol_slab).
 bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
                      cudaStream_t st);
-// nz_in / nz_out: the flags of the in and out buffers (null: no skipping).
-bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
-                      uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
-                      cudaStream_t st);
 // The sweep with its 3^4 box sum formed separably (blurType 2, flof_mg.cu):
 // s2 (a Vec4 grid of d's size) receives the 3x3 (x,y) sums, out the 1/81 of
 // their 3x3 (z,t) sums at unmarked interior cells.  Equal to the reference's

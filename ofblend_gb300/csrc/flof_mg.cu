@@ -281,15 +281,33 @@ __device__ __forceinline__ float4 xp_at(const float4 *__restrict__ x, const floa
                 __ldg(e1 + m.index((i - 1) >> 1, (j - 1) >> 1, (k - 1) >> 1, (l - 1) >> 1)));
 }
 
-// The same post-smoothing, one thread per interior (x, y, z) column walking
-// MG_TT consecutive t planes with y = x + P e1 at t-1, t, t+1 in registers
-// (the t neighbours cost no load).
+// The level-0 prolongation x += e1[parent] over the interior cells.
+__global__ void __launch_bounds__(MT)
+k_mg0_prolong(float4 *__restrict__ x, const float4 *__restrict__ e1, Dims4 d, BoxDecoder bx,
+              uint32_t nint, Dims4 m, const CGState *st) {
+  pdl_wait();
+  pdl_launch_dependents();
+  if (mg_stop(st)) return;
+  for (uint32_t n = blockIdx.x * blockDim.x + threadIdx.x; n < nint; n += gridDim.x * blockDim.x) {
+    int i, j, k, l;
+    bx.decode(n, i, j, k, l);
+    const idx_t id = d.index(i, j, k, l);
+    x[id] = f4_add(x[id],
+                   __ldg(e1 + m.index((i - 1) >> 1, (j - 1) >> 1, (k - 1) >> 1, (l - 1) >> 1)));
+  }
+}
+
+// The last level-0 sweep, z = y + omega D^-1 (b - A y) with y the prolonged
+// iterate (border cells zero), one thread per interior (x, y, z) column
+// walking MG_TT consecutive t planes with y at t-1, t, t+1 in registers (the
+// t neighbours cost no load); z . b for the PCG: init sets sigma (and
+// beta = 0), otherwise beta = z.b / sigma and sigma = z.b.
 constexpr int MG_TT = 8;
 __global__ void __launch_bounds__(MT)
 k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
-              const float4 *__restrict__ x, const float4 *__restrict__ e1, float4 *__restrict__ z,
-              Dims4 d, BoxDecoder bxyz, uint32_t nxyz, int tchunks, Dims4 m, float c0, float wS,
-              float omega, CGState *st, double *dpart, int init) {
+              const float4 *__restrict__ y, float4 *__restrict__ z, Dims4 d, BoxDecoder bxyz,
+              uint32_t nxyz, int tchunks, float c0, float wS, float omega, CGState *st,
+              double *dpart, int init) {
   pdl_wait();
   pdl_launch_dependents();
   if (mg_stop(st)) return;
@@ -298,6 +316,7 @@ k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
   FF dot = {0.f, 0.f};
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
   const uint32_t n = nxyz * (uint32_t)tchunks;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const uint32_t cell = q % nxyz, tc = q / nxyz;
     int i, j, k, unused;
@@ -305,28 +324,17 @@ k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
     const int l0 = 1 + (int)tc * MG_TT;
     const int l1 = min(l0 + MG_TT, d.t - 1);
     idx_t id = d.index(i, j, k, l0);
-    // parents of the cell and of its x, y, z neighbours (t varies below)
-    const int pi = (i - 1) >> 1, pj = (j - 1) >> 1, pk = (k - 1) >> 1;
-    const int pim = (i - 2) >> 1, pip = i >> 1, pjm = (j - 2) >> 1, pjp = j >> 1;
-    const int pkm = (k - 2) >> 1, pkp = k >> 1;
-    const bool hxm = i > 1, hxp = i < d.x - 2, hym = j > 1, hyp = j < d.y - 2;
-    const bool hzm = k > 1, hzp = k < d.z - 2;
-    auto yat = [&](idx_t c, int a, int bb, int cc, int dd) {
-      return f4_add(__ldg(x + c), __ldg(e1 + m.index(a, bb, cc, dd)));
-    };
-    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 ym = l0 > 1 ? yat(id - sT, pi, pj, pk, (l0 - 2) >> 1) : zero4;
-    float4 yc = yat(id, pi, pj, pk, (l0 - 1) >> 1);
+    // border cells of y hold zero, so the neighbour loads need no guards
+    float4 ym = __ldg(y + id - sT), yc = __ldg(y + id);
     for (int l = l0; l < l1; ++l, id += sT) {
-      const int pl = (l - 1) >> 1;
-      const float4 yp = l < d.t - 2 ? yat(id + sT, pi, pj, pk, l >> 1) : zero4;
-      float4 nb = f4_add(ym, yp);
-      if (hzm) nb = f4_add(nb, yat(id - sZ, pi, pj, pkm, pl));
-      if (hym) nb = f4_add(nb, yat(id - sY, pi, pjm, pk, pl));
-      if (hxm) nb = f4_add(nb, yat(id - 1, pim, pj, pk, pl));
-      if (hxp) nb = f4_add(nb, yat(id + 1, pip, pj, pk, pl));
-      if (hyp) nb = f4_add(nb, yat(id + sY, pi, pjp, pk, pl));
-      if (hzp) nb = f4_add(nb, yat(id + sZ, pi, pj, pkp, pl));
+      const float4 yp = __ldg(y + id + sT);
+      float4 nb = f4_add(ym, __ldg(y + id - sZ));
+      nb = f4_add(nb, __ldg(y + id - sY));
+      nb = f4_add(nb, __ldg(y + id - 1));
+      nb = f4_add(nb, __ldg(y + id + 1));
+      nb = f4_add(nb, __ldg(y + id + sY));
+      nb = f4_add(nb, __ldg(y + id + sZ));
+      nb = f4_add(nb, yp);
       const float4 gg = __ldg(g + id), bb = __ldg(b + id);
       const float4 res = f4_sub(bb, f4_axpy(-wS, nb, blk0_mul(gg, c0, yc)));
       const float4 zz = f4_axpy(omega, blk0_solve(gg, c0, res), yc);
@@ -879,10 +887,11 @@ void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0,
     const BoxDecoder bxyz = make_decoder(d.x - 2, d.y - 2, d.z - 2, 1, 1, 1, 0);
     const uint32_t nxyz = (uint32_t)((long long)(d.x - 2) * (d.y - 2) * (d.z - 2));
     const int tchunks = (d.t - 2 + MG_TT - 1) / MG_TT;
-    mg_launch(k_mg0_post_tw, grid_for((long long)nxyz * tchunks, MT, 8), MT, s, b0, g, x0, L[0].x,
-              z, d, bxyz, nxyz, tchunks, L[0].m, c0, wS, mp.omega0, st, dpart, init);
+    mg_launch(k_mg0_prolong, nb0, MT, s, x0, L[0].x, d, bx, nint, L[0].m, st);
+    mg_launch(k_mg0_post_tw, grid_for((long long)nxyz * tchunks, MT, 8), MT, s, b0, g, x0, z, d,
+              bxyz, nxyz, tchunks, c0, wS, mp.omega0, st, dpart, init);
+    nl_ += 2;
   }
-  ++nl_;
   if (launches) *launches += nl_ - 1;  // the caller counts one
 }
 

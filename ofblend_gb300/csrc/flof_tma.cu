@@ -81,8 +81,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+// The slab buffers are reused: a copy lands (async proxy) in a buffer the
+// block's threads read before (generic proxy).  The issuing thread passes the
+// barrier that ends those reads and then fences the two proxies, so that no
+// read still in flight sees the new slab.
 __device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map, int x, int y,
                                               int z, int t, uint64_t *bar) {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   asm volatile(
       "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(smem_u32(dst)),
@@ -113,7 +118,6 @@ __device__ __forceinline__ float4 unpack4(const P4 &v) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(r.z), "=f"(r.w) : "l"(v.hi));
   return r;
 }
-__device__ __forceinline__ float4 unpack4(const float4 &v) { return v; }
 __device__ __forceinline__ float4 mul4(float w, const float4 &a) {
   return make_float4(w * a.x, w * a.y, w * a.z, w * a.w);
 }
@@ -139,101 +143,33 @@ struct WTabT {
   float w[40];
 };
 
-// Zero-tracking flag bits of a sweep tile: some cell is nonzero, and some
-// cell on each face (x-, x+, y-, ... of the tile's extent) is nonzero.
-enum : uint32_t {
-  EXPOL_ANY = 1u,
-  EXPOL_FACE_XM = 2u, EXPOL_FACE_XP = 4u,
-  EXPOL_FACE_YM = 8u, EXPOL_FACE_YP = 16u,
-  EXPOL_FACE_ZM = 32u, EXPOL_FACE_ZP = 64u,
-  EXPOL_FACE_TM = 128u, EXPOL_FACE_TP = 256u,
-};
-__device__ __forceinline__ uint32_t expol_face_bits(const Dims4 &d, int x, int y, int z, int t,
-                                                   int ty, int dz, int dt) {
-  uint32_t b = EXPOL_ANY;
-  const int ix = x % TX, iy = y % ty, iz = z % dz, it = t % dt;
-  if (ix == 0) b |= EXPOL_FACE_XM;
-  if (ix == TX - 1 || x == d.x - 1) b |= EXPOL_FACE_XP;
-  if (iy == 0) b |= EXPOL_FACE_YM;
-  if (iy == ty - 1 || y == d.y - 1) b |= EXPOL_FACE_YP;
-  if (iz == 0) b |= EXPOL_FACE_ZM;
-  if (iz == dz - 1 || z == d.z - 1) b |= EXPOL_FACE_ZP;
-  if (it == 0) b |= EXPOL_FACE_TM;
-  if (it == dt - 1 || t == d.t - 1) b |= EXPOL_FACE_TP;
-  return b;
-}
-
-// MODE 0: Gaussian blur pass; MODE 1: extrapolation sweep.  A block computes
-// the outputs of DZ x DT consecutive (z, t) planes.  It walks the input slabs
-// (tt, zz) of the union of their neighbourhoods in lexicographic order; for a
-// fixed output plane (z_o, t_o) that order is the reference's (vt, zk) order
-// with vt = tt - t_o, zk = zz - z_o, so every output still adds its taps in
-// the reference's sequence while each slab is fetched once for all planes.
-template <int S, int MODE, class G>
+// The Gaussian blur pass.  A block computes the outputs of DZ x DT
+// consecutive (z, t) planes.  It walks the input slabs (tt, zz) of the union
+// of their neighbourhoods in lexicographic order; for a fixed output plane
+// (z_o, t_o) that order is the reference's (vt, zk) order with
+// vt = tt - t_o, zk = zz - z_o, so every output still adds its taps in the
+// reference's sequence while each slab is fetched once for all planes.
+template <int S, class G>
 __global__ void __launch_bounds__(G::NTHR, G::MINB)
-k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
-           int tiles_x, const float *__restrict__ wsum, const uint16_t *__restrict__ fixed,
-           WTabT wt, int zero_border, int *err, const uint32_t *__restrict__ nz_in,
-           uint32_t *__restrict__ nz_out, const uint32_t *__restrict__ keep_nz) {
+k_blur_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
+           int tiles_x, const float *__restrict__ wsum, WTabT wt, int zero_border, int *err) {
   constexpr int RY = G::RY, DT = G::DT, DZ = G::DZ, NS = G::NSTAGE;
   extern __shared__ __align__(128) unsigned char raw[];
   __shared__ __align__(8) uint64_t bar[NS];
   __shared__ float wsh[40];
 
   const int tile = blockIdx.x;
-  // this block's tile in the zero-tracking flags
-  auto self = [] { return ((long long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x; };
-  if (MODE == 1 && nz_in) {
-    const int ntile_xy = gridDim.x, tiles_y = ntile_xy / tiles_x;
-    // Skip when the input is zero over the tile and its 1-cell halo, and the
-    // tile is zero in the output: the sweep would write +0 over +0.  The halo
-    // cells a neighbour tile contributes lie on its face towards this tile
-    // (for a diagonal neighbour, on the face of the first axis it is offset
-    // along), so that face's flag decides.
-    int need = 0;
-    const int u = threadIdx.x;
-    if (u < 81) {
-      const int ox = u % 3 - 1, oy = (u / 3) % 3 - 1, oz = (u / 9) % 3 - 1, ot = u / 27 - 1;
-      const int ex = tile % tiles_x + ox, ey = tile / tiles_x + oy;
-      const int ez = (int)blockIdx.y + oz, et = (int)blockIdx.z + ot;
-      const uint32_t bit = ox ? (ox < 0 ? EXPOL_FACE_XP : EXPOL_FACE_XM)
-                         : oy ? (oy < 0 ? EXPOL_FACE_YP : EXPOL_FACE_YM)
-                         : oz ? (oz < 0 ? EXPOL_FACE_ZP : EXPOL_FACE_ZM)
-                         : ot ? (ot < 0 ? EXPOL_FACE_TP : EXPOL_FACE_TM)
-                              : EXPOL_ANY;
-      if (ex >= 0 && ex < tiles_x && ey >= 0 && ey < tiles_y && ez >= 0 &&
-          ez < (int)gridDim.y && et >= 0 && et < (int)gridDim.z)
-        need = (__ldg(nz_in + ((long long)et * gridDim.y + ez) * ntile_xy + ey * tiles_x + ex) &
-                bit) != 0;
-    } else if (u == 81) {
-      need = nz_out[self()] != 0;
-    }
-    if (!__syncthreads_or(need)) return;
-    // the tile's flag starts from its kept cells; threads that write a
-    // nonzero value raise it after the slab walk (whose barriers order the
-    // two stores)
-    if (threadIdx.x == 0) nz_out[self()] = keep_nz[self()];
-  }
   const int x0 = (tile % tiles_x) * TX, y0 = (tile / tiles_x) * G::TY;
   const int z0 = blockIdx.y * DZ, t0 = blockIdx.z * DT;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   const int x = x0 + tx;
-  // MODE 1: bit (oz*DT + o)*RY + q set = cell (x, y0+RY*ty+q, z0+oz, t0+o)
-  // keeps its value (loaded now, used after the slab walk)
-  unsigned keep = 0xffffu;
-  if (MODE == 1) {
-    const int ygroups = (d.y + RY - 1) / RY, zgroups = (d.z + DZ - 1) / DZ;
-    const int yg = y0 / RY + ty;
-    if (x < d.x && yg < ygroups)
-      keep = __ldg(fixed + (((size_t)blockIdx.z * zgroups + blockIdx.y) * ygroups + yg) * d.x + x);
-  }
 
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int b = 0; b < NS; ++b) mbar_init(&bar[b], 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  if (MODE == 0 && threadIdx.x < 40) wsh[threadIdx.x] = wt.w[threadIdx.x];
+  if (threadIdx.x < 40) wsh[threadIdx.x] = wt.w[threadIdx.x];
   __syncthreads();
 
   constexpr int KZ = DZ + 2 * S;
@@ -251,8 +187,7 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       if (p < NP) issue(p);
   }
 
-  // accumulator / slab element: float4 for the blur, packed pairs for the sweep
-  typedef typename std::conditional<MODE == 0, float4, P4>::type V4;
+  typedef float4 V4;
   V4 val[DZ][DT][RY];
 #pragma unroll
   for (int oz = 0; oz < DZ; ++oz)
@@ -291,36 +226,26 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
         for (int o = 0; o < DT; ++o) {
           const int vt = vt0 - o;
           if (vt < -S || vt > S) continue;
-          if constexpr (MODE == 0) {
-            // Output rows at y offsets +-ay use the same weights, so the
-            // rounded products w * a are formed once per |yj| and added to
-            // each of those rows in the usual xi order.
+          // Output rows at y offsets +-ay use the same weights, so the
+          // rounded products w * a are formed once per |yj| and added to
+          // each of those rows in the usual xi order.
 #pragma unroll
-            for (int ay = 0; ay <= S; ++ay) {
-              bool used = false;
+          for (int ay = 0; ay <= S; ++ay) {
+            bool used = false;
 #pragma unroll
-              for (int q = 0; q < RY; ++q) used |= (k - q - S == ay) || (k - q - S == -ay);
-              if (!used) continue;
-              const int base = vt * vt + zk * zk + ay * ay;
-              float4 prod[2 * S + 1];
+            for (int q = 0; q < RY; ++q) used |= (k - q - S == ay) || (k - q - S == -ay);
+            if (!used) continue;
+            const int base = vt * vt + zk * zk + ay * ay;
+            float4 prod[2 * S + 1];
 #pragma unroll
-              for (int xi = -S; xi <= S; ++xi)
-                prod[xi + S] = mul4(wsh[base + xi * xi], a[xi + S]);
-#pragma unroll
-              for (int q = 0; q < RY; ++q) {
-                const int yj = k - q - S;
-                if (yj != ay && yj != -ay) continue;
-#pragma unroll
-                for (int xi = -S; xi <= S; ++xi) add4(val[oz][o][q], prod[xi + S]);
-              }
-            }
-          } else {
+            for (int xi = -S; xi <= S; ++xi)
+              prod[xi + S] = mul4(wsh[base + xi * xi], a[xi + S]);
 #pragma unroll
             for (int q = 0; q < RY; ++q) {
               const int yj = k - q - S;
-              if (yj < -S || yj > S) continue;
+              if (yj != ay && yj != -ay) continue;
 #pragma unroll
-              for (int xi = -S; xi <= S; ++xi) acc4(val[oz][o][q], a[xi + S]);
+              for (int xi = -S; xi <= S; ++xi) add4(val[oz][o][q], prod[xi + S]);
             }
           }
         }
@@ -330,7 +255,6 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
 
   if (x >= d.x) return;
-  uint32_t fbits = 0;  // MODE 1: face bits of the nonzero values this thread writes
   constexpr int P1 = (S + 1) * (S + 1);
 #pragma unroll
   for (int oz = 0; oz < DZ; ++oz) {
@@ -341,40 +265,22 @@ k_slab_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       const int t = t0 + o;
       if (t >= d.t) break;
       const bool zt_inner = z >= 1 && z < d.z - 1 && t >= 1 && t < d.t - 1;
-      const int code_zt =
-          MODE == 0 ? ((clip_code_t<S>(t, d.t) * P1 + clip_code_t<S>(z, d.z)) * P1) : 0;
+      const int code_zt = (clip_code_t<S>(t, d.t) * P1 + clip_code_t<S>(z, d.z)) * P1;
 #pragma unroll
       for (int q = 0; q < RY; ++q) {
         const int y = y0 + RY * ty + q;
         if (y >= d.y) continue;
         const idx_t id = d.index(x, y, z, t);
-        const float4 v = unpack4(val[oz][o][q]);
-        if (MODE == 0) {
-          if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
-            if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
-            continue;
-          }
-          const float ws =
-              __ldg(wsum + (code_zt + clip_code_t<S>(y, d.y)) * P1 + clip_code_t<S>(x, d.x));
-          dst[id] = make_float4(v.x / ws, v.y / ws, v.z / ws, v.w / ws);
-        } else {
-          if (keep >> ((oz * DT + o) * RY + q) & 1u) continue;
-          const float4 r =
-              make_float4(mul_inv81(v.x), mul_inv81(v.y), mul_inv81(v.z), mul_inv81(v.w));
-          // nonzero unless all four are +-0 (a NaN counts as nonzero)
-          if ((__float_as_uint(r.x) | __float_as_uint(r.y) | __float_as_uint(r.z) |
-               __float_as_uint(r.w)) & 0x7fffffffu)
-            fbits |= expol_face_bits(d, x, y, z, t, G::TY, DZ, DT);
-          dst[id] = r;
+        const float4 v = val[oz][o][q];
+        if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
+          if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+          continue;
         }
+        const float ws =
+            __ldg(wsum + (code_zt + clip_code_t<S>(y, d.y)) * P1 + clip_code_t<S>(x, d.x));
+        dst[id] = make_float4(v.x / ws, v.y / ws, v.z / ws, v.w / ws);
       }
     }
-  }
-  if (MODE == 1 && nz_in) {
-    // threads past the grid's end returned above; one atomic per warp
-    const unsigned act = __activemask();
-    const uint32_t w = __reduce_or_sync(act, fbits);
-    if (w && (threadIdx.x & 31) == __ffs(act) - 1) atomicOr(nz_out + self(), w);
   }
 }
 
@@ -549,20 +455,17 @@ bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) 
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int S, int MODE, class G>
-bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
-                const uint16_t *fixed, const float *w, int zero_border, int *err,
-                cudaStream_t st, const uint32_t *nz_in = nullptr, uint32_t *nz_out = nullptr,
-                const uint32_t *keep_nz = nullptr) {
+template <int S, class G>
+bool launch_blur(const float4 *src, float4 *dst, Dims4 d, const float *wsum, const float *w,
+                 int zero_border, int *err, cudaStream_t st) {
   const int tgroups = (d.t + G::DT - 1) / G::DT, zgroups = (d.z + G::DZ - 1) / G::DZ;
   if (zgroups > 65535 || tgroups > 65535) return false;
   CUtensorMap map;
   if (!encode_slab_map(&map, src, d, G::W, G::H)) return false;
   const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + G::TY - 1) / G::TY;
   dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
-  const size_t smem = G::SMEM;
   static const bool attr = [] {
-    if (cudaFuncSetAttribute(k_slab_tma<S, MODE, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_blur_tma<S, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)G::SMEM) != cudaSuccess) {
       cudaGetLastError();
       return false;
@@ -572,8 +475,8 @@ bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
   if (!attr) return false;
   WTabT wt;
   for (int i = 0; i < 40; ++i) wt.w[i] = (w && i <= 4 * S * S) ? w[i] : 0.f;
-  k_slab_tma<S, MODE, G><<<grid, G::NTHR, smem, st>>>(map, dst, d, tiles_x, wsum, fixed, wt,
-                                                     zero_border, err, nz_in, nz_out, keep_nz);
+  k_blur_tma<S, G><<<grid, G::NTHR, G::SMEM, st>>>(map, dst, d, tiles_x, wsum, wt, zero_border,
+                                                   err);
   return true;
 }
 
@@ -581,12 +484,8 @@ bool launch_tma(const float4 *src, float4 *dst, Dims4 d, const float *wsum,
 
 bool launch_gauss_tma(const float4 *src, float4 *dst, Dims4 d, int s, const float *wtab,
                       const float *wsum_dev, int zero_border, int *err, cudaStream_t st) {
-  if (s == 1)
-    return launch_tma<1, 0, BlurGeom<1>>(src, dst, d, wsum_dev, nullptr, wtab, zero_border, err,
-                                         st);
-  if (s == 2)
-    return launch_tma<2, 0, BlurGeom<2>>(src, dst, d, wsum_dev, nullptr, wtab, zero_border, err,
-                                         st);
+  if (s == 1) return launch_blur<1, BlurGeom<1>>(src, dst, d, wsum_dev, wtab, zero_border, err, st);
+  if (s == 2) return launch_blur<2, BlurGeom<2>>(src, dst, d, wsum_dev, wtab, zero_border, err, st);
   return false;
 }
 
@@ -595,14 +494,10 @@ namespace {
 // One 16-bit word per sweep thread: (x, y group of RY rows, z group of DZ, t
 // group of DT), x fastest.  A bit is set for each of the thread's cells that
 // the sweep leaves alone: marked, outside the interior (knCvExpolBlur4d runs
-// over bnd = 1), or past the grid's end.  With flag arrays, the word's cells
-// also raise the zero-tracking flags of their sweep tile.
-__global__ void k_expol_mask(const float *__restrict__ mark, const float4 *__restrict__ src,
-                             uint16_t *__restrict__ mask, uint32_t *nz_a, uint32_t *nz_b,
-                             uint32_t *keep_nz, Dims4 d, int ygroups, int zgroups, int tiles_x,
-                             int tiles_y, long long nwords) {
+// over bnd = 1), or past the grid's end.
+__global__ void k_expol_mask(const float *__restrict__ mark, uint16_t *__restrict__ mask, Dims4 d,
+                             int ygroups, int zgroups, long long nwords) {
   constexpr int RY = ExpolGeom::RY, DT = ExpolGeom::DT, DZ = ExpolGeom::DZ;
-  constexpr int YG_PER_TILE = ExpolGeom::TY / RY;
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nwords;
        w += (long long)gridDim.x * blockDim.x) {
     const int x = (int)(w % d.x);
@@ -612,7 +507,6 @@ __global__ void k_expol_mask(const float *__restrict__ mark, const float4 *__res
     const int zg = (int)(r % zgroups);
     const int tg = (int)(r / zgroups);
     unsigned bits = 0;
-    uint32_t any = 0, anyKeep = 0;  // face bits of the nonzero cells (all / kept)
     for (int oz = 0; oz < DZ; ++oz)
       for (int o = 0; o < DT; ++o)
         for (int q = 0; q < RY; ++q) {
@@ -621,29 +515,12 @@ __global__ void k_expol_mask(const float *__restrict__ mark, const float4 *__res
             bits |= 1u << ((oz * DT + o) * RY + q);
             continue;
           }
-          const idx_t id = d.index(x, y, z, t);
           const bool inner = x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1 && z >= 1 &&
                              z < d.z - 1 && t >= 1 && t < d.t - 1;
-          const bool kept = !inner || __ldg(mark + id) != 0.f;
-          if (kept) bits |= 1u << ((oz * DT + o) * RY + q);
-          if (nz_a) {
-            const float4 v = __ldg(src + id);
-            if ((v.x != 0.f) | (v.y != 0.f) | (v.z != 0.f) | (v.w != 0.f)) {
-              const uint32_t fb = expol_face_bits(d, x, y, z, t, ExpolGeom::TY, DZ, DT);
-              any |= fb;
-              if (kept) anyKeep |= fb;
-            }
-          }
+          if (!inner || __ldg(mark + d.index(x, y, z, t)) != 0.f)
+            bits |= 1u << ((oz * DT + o) * RY + q);
         }
     mask[w] = (uint16_t)bits;
-    if (any) {
-      const long long f =
-          ((long long)tg * zgroups + zg) * ((long long)tiles_x * tiles_y) +
-          (long long)(yg / YG_PER_TILE) * tiles_x + x / TX;
-      atomicOr(nz_a + f, any);
-      atomicOr(nz_b + f, any);
-      if (anyKeep) atomicOr(keep_nz + f, anyKeep);
-    }
   }
 }
 
@@ -654,19 +531,11 @@ size_t expol_mask_words(Dims4 d) {
          ((d.z + ExpolGeom::DZ - 1) / ExpolGeom::DZ) * ((d.t + ExpolGeom::DT - 1) / ExpolGeom::DT);
 }
 
-size_t expol_tiles(Dims4 d) {
-  return (size_t)((d.x + TX - 1) / TX) * ((d.y + ExpolGeom::TY - 1) / ExpolGeom::TY) *
-         ((d.z + ExpolGeom::DZ - 1) / ExpolGeom::DZ) * ((d.t + ExpolGeom::DT - 1) / ExpolGeom::DT);
-}
-
-void launch_expol_mask(const float *mark, const float4 *src, uint16_t *mask, uint32_t *nz_a,
-                       uint32_t *nz_b, uint32_t *keep_nz, Dims4 d, cudaStream_t st) {
+void launch_expol_mask(const float *mark, uint16_t *mask, Dims4 d, cudaStream_t st) {
   const long long n = (long long)expol_mask_words(d);
   const int ygroups = (d.y + ExpolGeom::RY - 1) / ExpolGeom::RY;
   const int zgroups = (d.z + ExpolGeom::DZ - 1) / ExpolGeom::DZ;
-  const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + ExpolGeom::TY - 1) / ExpolGeom::TY;
-  k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, src, mask, nz_a, nz_b, keep_nz, d,
-                                                 ygroups, zgroups, tiles_x, tiles_y, n);
+  k_expol_mask<<<grid_for(n, 256), 256, 0, st>>>(mark, mask, d, ygroups, zgroups, n);
 }
 
 bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
@@ -688,13 +557,6 @@ bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 
   dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
   k_expol_tw<<<grid, 32 * ETW_NW, ETW_SMEM, st>>>(map, out, d, tiles_x, mask, err);
   return true;
-}
-
-bool launch_expol_tma(const float4 *in, float4 *out, const uint16_t *mask, const uint32_t *nz_in,
-                      uint32_t *nz_out, const uint32_t *keep_nz, Dims4 d, int *err,
-                      cudaStream_t st) {
-  return launch_tma<1, 1, ExpolGeom>(in, out, d, nullptr, mask, nullptr, 0, err, st, nz_in,
-                                     nz_out, keep_nz);
 }
 
 }  // namespace flof
