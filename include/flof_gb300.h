@@ -171,8 +171,12 @@ FLOF_API const char *flof_kernel_class_name(int cls);
  *   metric serially in calcLsDiffTempl's loop order (:895-927), so that
  *   whole solves equal the reference's bit for bit.  One thread forms each
  *   sum: for parity checks on grids of a few million cells, not for speed.
- *   0 (default): the parallel kernels. */
-enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3, FLOF_OPT_STRICT = 4 };
+ *   0 (default): the parallel kernels.
+ * FLOF_OPT_SLAB_TMA: 1 (default) the Vec4 Gaussian blur and the extrapolation
+ *   sweeps of corrVelsOf4d use the TMA slab kernels; 0 their plain-load
+ *   counterparts, which take the same sums in the same order (equal results;
+ *   for checking one against the other). */
+enum { FLOF_OPT_CFL_SYNC = 2, FLOF_OPT_AUTOTUNE = 3, FLOF_OPT_STRICT = 4, FLOF_OPT_SLAB_TMA = 5 };
 FLOF_API int flof_ctx_set_option(flof_ctx *ctx, int option, int value);
 /* Parameters of the multigrid V-cycle of FLOF_SOLVER_MG (no reference
  * counterpart): damping of the block-Jacobi sweeps on the system's own grid

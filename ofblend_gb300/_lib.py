@@ -17,6 +17,7 @@ FLOF_VEC4 = 8
 FLOF_OPT_CFL_SYNC = 2
 FLOF_OPT_AUTOTUNE = 3
 FLOF_OPT_STRICT = 4
+FLOF_OPT_SLAB_TMA = 5
 FLOF_PRECISION_FP32 = 0
 FLOF_PRECISION_MIXED = 1
 FLOF_SOLVER_PCG = 0

@@ -29,6 +29,7 @@ flof_ctx *worker(flof_ctx *c, size_t q) {
     w->cfl_force_sync = c->cfl_force_sync;
     w->autotune = c->autotune;
     w->strict = c->strict;
+    w->slab_tma = c->slab_tma;
     w->mg = c->mg;
     w->tune_owner = c;
     c->workers.push_back(w);

@@ -161,7 +161,7 @@ void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurTyp
         float *dst = pass == 0 ? tmp.f() : a;
         const int zb = pass == 0 ? 1 : 0;
         bool tma = false;
-        if (nc == 4)
+        if (nc == 4 && c->slab_tma)
           KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
               tma = launch_gauss_tma((const float4 *)src, (float4 *)dst, d, s, wtab, ws, zb,
                                      c->dev_err, c->stream));
@@ -179,15 +179,16 @@ void gauss_blur(flof_ctx *c, float *a, Dims4 d, int nc, float sigma, int blurTyp
     float w1[8];
     for (int q = 0; q <= s; ++q)
       w1[q] = (float)exp((double)(-(float)(q * q)) / (2. * (double)sigma * (double)sigma));
-    DBuf t1(c, nb), t2(c, nb), t3(c, nb);
-    KL(c, launch_gauss_sep_pass(a, t1.f(), d, nc, 0, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t1.f(), t2.f(), d, nc, 1, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t2.f(), t1.f(), d, nc, 2, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t1.f(), t3.f(), d, nc, 3, s, w1, 1, c->stream));
-    KL(c, launch_gauss_sep_pass(t3.f(), t1.f(), d, nc, 0, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t1.f(), t2.f(), d, nc, 1, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t2.f(), t1.f(), d, nc, 2, s, w1, 0, c->stream));
-    KL(c, launch_gauss_sep_pass(t1.f(), a, d, nc, 3, s, w1, 2, c->stream));
+    // the reference's two passes: a -> t2 (zero ring), t2 -> a (ring kept)
+    DBuf t1(c, nb), t2(c, nb);
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_sep_pair(a, t1.f(), d, nc, 0, s, w1, 0, c->stream));
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_sep_pair(t1.f(), t2.f(), d, nc, 1, s, w1, 1, c->stream));
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_sep_pair(t2.f(), t1.f(), d, nc, 0, s, w1, 0, c->stream));
+    KLP(c, KC_BLUR, d.x, d.cells() * nc * 8,
+        launch_gauss_sep_pair(t1.f(), a, d, nc, 1, s, w1, 2, c->stream));
   }
 }
 
@@ -603,23 +604,30 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
       // The sweeps only rewrite unmarked interior cells; both buffers carry
       // the projected values everywhere else (the reference's tmp copy).
       CK(cudaMemcpyAsync(B, A, vec_bytes(d), cudaMemcpyDeviceToDevice, c->stream));
-      if (blurType != FLOF_BLUR_GAUSS_SEPARABLE)  // the separable sweep reads the marker
+      if (c->slab_tma)  // the plain-load sweeps read the marker
         KLP(c, KC_EXPOL_MASK, d.x, d.cells() * 4,
             launch_expol_mask(marker.f(), (uint16_t *)mask.p, d, c->stream));
     }
+    const uint16_t *keep = (const uint16_t *)mask.p;
     for (int s = 0; s < doCvExtrapol; ++s) {
-      if (blurType == FLOF_BLUR_GAUSS_SEPARABLE) {
-        if (!s2.p) s2 = DBuf(c, vec_bytes(d));
-        KLP(c, KC_EXPOL, d.x, d.cells() * 68,
-            launch_expol_sep(A, B, s2.v(), marker.f(), d, c->stream));
-        std::swap(A, B);
-        continue;
-      }
       bool tma = false;
-      KLP(c, KC_EXPOL, d.x, d.cells() * 32,
-          tma = launch_expol_tw(A, B, (const uint16_t *)mask.p, d, c->dev_err, c->stream));
-      if (!tma)
-        KLP(c, KC_EXPOL, d.x, d.cells() * 36, launch_expol_slab(A, B, marker.f(), d, c->stream));
+      if (blurType == FLOF_BLUR_GAUSS_SEPARABLE) {
+        if (c->slab_tma)
+          KLP(c, KC_EXPOL, d.x, d.cells() * 32,
+              tma = launch_expol_sep_tw(A, B, keep, d, c->dev_err, c->stream));
+        if (!tma) {
+          if (!s2.p) s2 = DBuf(c, vec_bytes(d));
+          KLP(c, KC_EXPOL, d.x, d.cells() * 68,
+              launch_expol_sep(A, B, s2.v(), marker.f(), d, c->stream));
+        }
+      } else {
+        if (c->slab_tma)
+          KLP(c, KC_EXPOL, d.x, d.cells() * 32,
+              tma = launch_expol_tw(A, B, keep, d, c->dev_err, c->stream));
+        if (!tma)
+          KLP(c, KC_EXPOL, d.x, d.cells() * 36,
+              launch_expol_slab(A, B, marker.f(), d, c->stream));
+      }
       std::swap(A, B);
     }
     if (postVelBlur > 1e-6f) gauss_blur(c, (float *)A, d, 4, (float)(0.5 * postVelBlur), blurType);
@@ -1010,6 +1018,10 @@ FLOF_API int flof_ctx_set_option(flof_ctx *c, int option, int value) {
       need(value == 0 || value == 1, "FLOF_OPT_STRICT takes 0 or 1");
       c->strict = value;
       for (flof_ctx *w : c->workers) w->strict = value;
+    } else if (option == FLOF_OPT_SLAB_TMA) {
+      need(value == 0 || value == 1, "FLOF_OPT_SLAB_TMA takes 0 or 1");
+      c->slab_tma = value;
+      for (flof_ctx *w : c->workers) w->slab_tma = value;
     } else if (option == FLOF_OPT_AUTOTUNE) {
       need(value == 0 || value == 1, "FLOF_OPT_AUTOTUNE takes 0 or 1");
       c->autotune = value;

@@ -156,6 +156,9 @@ struct flof_ctx {
   int autotune = 0;
   // FLOF_OPT_STRICT: the reference's PCG and error-metric arithmetic
   int strict = 0;
+  // FLOF_OPT_SLAB_TMA: 1 the TMA slab kernels for the Vec4 blur and the
+  // extrapolation sweeps, 0 their plain-load counterparts
+  int slab_tma = 1;
   // parameters of the multigrid preconditioner (FLOF_SOLVER_MG) and the
   // number of its solves the plain PCG had to finish
   flof::MGParams mg;

@@ -257,12 +257,12 @@ void launch_of_copy_back(const float4 *x, float4 *vel, long long cells,
 // distance (host-computed, as the reference's float(exp(double))).
 void launch_gauss_pass(const float *src, float *dst, Dims4 d, int nc, int s,
                        const float *wtab, int zero_border, cudaStream_t st);
-// Separable variant (blurType 2): one axis of the 4x1D stencil with
-// in-bounds normalisation; not bitwise equal to the reference.  border_mode
-// 0 writes every cell, 1 interior cells plus a zero ring, 2 interior only.
-void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
-                           int axis, int s, const float *w1d, int border_mode,
-                           cudaStream_t st);
+// Separable variant (blurType 2): two axes of the 4x1D stencil with
+// in-bounds normalisation, x then y (zt = 0, every cell) or z then t (zt = 1,
+// interior cells; border_mode 1 zeros the one-cell ring, 2 leaves it alone);
+// equal to the reference's blur up to rounding.
+void launch_gauss_sep_pair(const float *src, float *dst, Dims4 d, int nc, int zt, int s,
+                           const float *w1d, int border_mode, cudaStream_t st);
 
 // Shared-memory slab versions (flof_stencil.cu) of the blur pass for radius
 // 1 and 2 and of the extrapolation sweep; same results bit for bit.
@@ -302,6 +302,10 @@ bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 
 // 81-term sum up to rounding.
 void launch_expol_sep(const float4 *in, float4 *out, float4 *s2, const float *mark, Dims4 d,
                       cudaStream_t s);
+// The separable sweep in one TMA pass walking t, with the same sums in the
+// same order as launch_expol_sep (equal bits); false when TMA is unavailable.
+bool launch_expol_sep_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                         cudaStream_t st);
 
 // ---- projection correction ------------------------------------------------------
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,

@@ -934,6 +934,9 @@ void launch_mgcg_direction(float4 *p, const float4 *z, Dims4 d, const CGState *s
 //                 every z, t;
 //   out         = 1/81 of the 3x3 (z,t) box sum of S2, each thread walking
 //                 t with the z sums of t-1, t, t+1 in registers.
+// Every 3-term sum is (a-1 + a0) + a+1, x first, then y, z and t: the order
+// of the one-pass TMA sweep (k_expol_sep_tw, flof_tma.cu), which this pair
+// of kernels stands in for where TMA is unavailable.
 // Marked and border cells are not written: both sweep buffers hold their
 // values.
 // ---------------------------------------------------------------------------
@@ -947,13 +950,10 @@ k_sep_xy(const float4 *__restrict__ src, float4 *__restrict__ s2, Dims4 d, BoxDe
     int i, j, k, l;
     bx.decode(q, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy) {
-      const idx_t r = id + dy * sY;
-      s = f4_add(s, f4_add(f4_add(__ldg(src + r - 1), __ldg(src + r)), __ldg(src + r + 1)));
-    }
-    s2[id] = s;
+    auto xsum = [&](idx_t r) {
+      return f4_add(f4_add(__ldg(src + r - 1), __ldg(src + r)), __ldg(src + r + 1));
+    };
+    s2[id] = f4_add(f4_add(xsum(id - sY), xsum(id)), xsum(id + sY));
   }
 }
 

@@ -724,65 +724,174 @@ void launch_gauss_pass(const float *src, float *dst, Dims4 d, int nc, int s,
     k_gauss_pass<1><<<nb, NT, 0, st>>>(src, dst, d, bx, s, wt, zero_border);
 }
 
-// One axis of the separable blur: dst = sum_in_bounds w1d * src / sum w1d.
-// border_mode: 0 every cell, 1 interior cells and a zero ring, 2 interior
-// cells only (the ring keeps its previous values).
+// The separable blur (blurType 2).  Along one axis, the sum at coordinate c
+// is sum_o w|o| src(c + o) over the in-range taps o = -S..S in increasing o,
+// each added by one fused multiply-add, times 1 / (the in-range weights
+// added in the same order): the 1D normalised Gaussian with clipping.  The
+// four axes are applied in the order x, y, z, t by two kernels: one forms
+// the y sums of x sums within each (z, t) plane, the other the t sums of z
+// sums, each thread walking a run of y rows or t planes with the 2S + 1
+// inner sums it needs in a register ring.  Every intermediate value is the
+// single-axis pass's, rounded once to float, so the pair equals four
+// single-axis passes; the 4D weight of the reference's blur is the product
+// of the 1D weights and its in-bounds box the product of the 1D ranges, so
+// the result equals the direct normalised stencil up to rounding.
+struct W1 {
+  float w[7];  // 1D weight by tap distance, S <= 6
+};
 template <int NC>
-__global__ void k_gauss_sep(const float *__restrict__ src, float *__restrict__ dst,
-                            Dims4 d, BoxDecoder bx, int axis, int s, WTab w1,
-                            int border_mode) {
-  const uint32_t n = (uint32_t)d.cells();
-  const int ext[4] = {d.x, d.y, d.z, d.t};
-  const idx_t str[4] = {1, d.x, d.sz(), d.st()};
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n;
-       q += gridDim.x * blockDim.x) {
-    int c[4];
-    bx.decode(q, c[0], c[1], c[2], c[3]);
-    if (border_mode != 0 && !in_bounds(d, c[0], c[1], c[2], c[3], 1)) {
-      if (border_mode == 1) {
-        if (NC == 4) ((float4 *)dst)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        else dst[q] = 0.f;
-      }
-      continue;
+__device__ __forceinline__ float4 ld_nc(const float *p, idx_t i) {
+  if (NC == 4) return __ldg((const float4 *)p + i);
+  return make_float4(__ldg(p + i), 0.f, 0.f, 0.f);
+}
+template <int NC>
+__device__ __forceinline__ void st_nc(float *p, idx_t i, float4 v) {
+  if (NC == 4) ((float4 *)p)[i] = v;
+  else p[i] = v.x;
+}
+__device__ __forceinline__ void fma4(float4 &v, float w, const float4 &a) {
+  v.x = __fmaf_rn(w, a.x, v.x);
+  v.y = __fmaf_rn(w, a.y, v.y);
+  v.z = __fmaf_rn(w, a.z, v.z);
+  v.w = __fmaf_rn(w, a.w, v.w);
+}
+__device__ __forceinline__ float4 scale4(const float4 &v, float s) {
+  return make_float4(v.x * s, v.y * s, v.z * s, v.w * s);
+}
+// 1 / (sum of the in-range 1D weights around c on an axis of n cells)
+template <int S>
+__device__ __forceinline__ float sep_inv(const W1 &w, int c, int n) {
+  float weight = 0.f;
+#pragma unroll
+  for (int o = -S; o <= S; ++o)
+    if (c + o >= 0 && c + o < n) weight += w.w[o < 0 ? -o : o];
+  return 1.0f / weight;
+}
+// the normalised 1D sum of the ring r (values at c - S .. c + S)
+template <int S>
+__device__ __forceinline__ float4 sep_ring(const W1 &w, const float4 (&r)[2 * S + 1], int c, int n) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int o = -S; o <= S; ++o)
+    if (c + o >= 0 && c + o < n) fma4(v, w.w[o < 0 ? -o : o], r[o + S]);
+  return scale4(v, sep_inv<S>(w, c, n));
+}
+
+constexpr int SEP_RUN = 16;  // y rows or t planes walked per thread
+
+// dst(x, y, z, t) = the y sum of the x sums, every cell
+template <int NC, int S>
+__global__ void __launch_bounds__(NT)
+k_blur_sep_xy(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W1 w,
+              uint32_t n) {
+  const idx_t sY = d.x;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int x = (int)(q % (uint32_t)d.x);
+    uint32_t r = q / (uint32_t)d.x;
+    const int z = (int)(r % (uint32_t)d.z);
+    r /= (uint32_t)d.z;
+    const int t = (int)(r % (uint32_t)d.t);
+    const int ya = (int)(r / (uint32_t)d.t) * SEP_RUN, yb = min(ya + SEP_RUN, d.y);
+    const idx_t plane = d.index(x, 0, z, t);
+    const float ix = sep_inv<S>(w, x, d.x);
+    auto xsum = [&](int y) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (y < 0 || y >= d.y) return v;  // out of range: never used
+      const idx_t id = plane + y * sY;
+#pragma unroll
+      for (int o = -S; o <= S; ++o)
+        if (x + o >= 0 && x + o < d.x) fma4(v, w.w[o < 0 ? -o : o], ld_nc<NC>(src, id + o));
+      return scale4(v, ix);
+    };
+    float4 ring[2 * S + 1];
+#pragma unroll
+    for (int k = 1; k <= 2 * S; ++k) ring[k] = xsum(ya - S - 1 + k);
+    for (int y = ya; y < yb; ++y) {
+#pragma unroll
+      for (int k = 0; k < 2 * S; ++k) ring[k] = ring[k + 1];
+      ring[2 * S] = xsum(y + S);
+      st_nc<NC>(dst, plane + y * sY, sep_ring<S>(w, ring, y, d.y));
     }
-    const int x0 = c[axis];
-    float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
-    float weight = 0.f;
-    for (int o = -s; o <= s; ++o) {
-      const int xx = x0 + o;
-      if (xx < 0 || xx >= ext[axis]) continue;
-      const float w = w1.w[o < 0 ? -o : o];
-      weight += w;
-      const idx_t id = (idx_t)q + (idx_t)o * str[axis];
-      if (NC == 4) {
-        const float4 a = __ldg((const float4 *)src + id);
-        val.x += w * a.x;
-        val.y += w * a.y;
-        val.z += w * a.z;
-        val.w += w * a.w;
-      } else {
-        val.x += w * __ldg(src + id);
-      }
-    }
-    const float inv = 1.0f / weight;
-    if (NC == 4)
-      ((float4 *)dst)[q] = make_float4(val.x * inv, val.y * inv, val.z * inv, val.w * inv);
-    else
-      dst[q] = val.x * inv;
   }
 }
 
-void launch_gauss_sep_pass(const float *src, float *dst, Dims4 d, int nc,
-                           int axis, int s, const float *w1d, int border_mode,
-                           cudaStream_t st) {
-  WTab wt;
-  for (int q = 0; q < 160; ++q) wt.w[q] = q <= s ? w1d[q] : 0.f;
-  BoxDecoder bx = make_decoder(d.x, d.y, d.z, 0, 0, 0, 0);
-  const int nb = grid_for(d.cells(), NT, 8);
-  if (nc == 4)
-    k_gauss_sep<4><<<nb, NT, 0, st>>>(src, dst, d, bx, axis, s, wt, border_mode);
-  else
-    k_gauss_sep<1><<<nb, NT, 0, st>>>(src, dst, d, bx, axis, s, wt, border_mode);
+// dst(x, y, z, t) = the t sum of the z sums at interior cells; border_mode 1
+// writes zeros on the one-cell ring, 2 leaves it alone
+template <int NC, int S>
+__global__ void __launch_bounds__(NT)
+k_blur_sep_zt(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W1 w,
+              int border_mode, uint32_t n) {
+  const idx_t sZ = d.sz(), sT = d.st();
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int x = (int)(q % (uint32_t)d.x);
+    uint32_t r = q / (uint32_t)d.x;
+    const int y = (int)(r % (uint32_t)d.y);
+    r /= (uint32_t)d.y;
+    const int z = (int)(r % (uint32_t)d.z);
+    const int ta = (int)(r / (uint32_t)d.z) * SEP_RUN, tb = min(ta + SEP_RUN, d.t);
+    const idx_t col = d.index(x, y, z, 0);
+    const bool ring_xyz = x < 1 || x >= d.x - 1 || y < 1 || y >= d.y - 1 || z < 1 || z >= d.z - 1;
+    if (ring_xyz) {
+      if (border_mode == 1)
+        for (int t = ta; t < tb; ++t) st_nc<NC>(dst, col + t * sT, make_float4(0.f, 0.f, 0.f, 0.f));
+      continue;
+    }
+    const float iz = sep_inv<S>(w, z, d.z);
+    auto zsum = [&](int t) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t < 0 || t >= d.t) return v;  // out of range: never used
+      const idx_t id = col + t * sT;
+#pragma unroll
+      for (int o = -S; o <= S; ++o)
+        if (z + o >= 0 && z + o < d.z) fma4(v, w.w[o < 0 ? -o : o], ld_nc<NC>(src, id + o * sZ));
+      return scale4(v, iz);
+    };
+    float4 ring[2 * S + 1];
+#pragma unroll
+    for (int k = 1; k <= 2 * S; ++k) ring[k] = zsum(ta - S - 1 + k);
+    for (int t = ta; t < tb; ++t) {
+#pragma unroll
+      for (int k = 0; k < 2 * S; ++k) ring[k] = ring[k + 1];
+      ring[2 * S] = zsum(t + S);
+      if (t < 1 || t >= d.t - 1) {
+        if (border_mode == 1) st_nc<NC>(dst, col + t * sT, make_float4(0.f, 0.f, 0.f, 0.f));
+        continue;
+      }
+      st_nc<NC>(dst, col + t * sT, sep_ring<S>(w, ring, t, d.t));
+    }
+  }
+}
+
+template <int NC, int S>
+void launch_sep_pair(const float *src, float *dst, Dims4 d, int zt, const W1 &w, int border_mode,
+                     cudaStream_t st) {
+  if (!zt) {
+    const uint32_t n = (uint32_t)((long long)d.x * d.z * d.t * ((d.y + SEP_RUN - 1) / SEP_RUN));
+    k_blur_sep_xy<NC, S><<<grid_for(n, NT, 8), NT, 0, st>>>(src, dst, d, w, n);
+  } else {
+    const uint32_t n = (uint32_t)((long long)d.x * d.y * d.z * ((d.t + SEP_RUN - 1) / SEP_RUN));
+    k_blur_sep_zt<NC, S><<<grid_for(n, NT, 8), NT, 0, st>>>(src, dst, d, w, border_mode, n);
+  }
+}
+template <int NC>
+void launch_sep_pair_nc(const float *src, float *dst, Dims4 d, int zt, int s, const W1 &w,
+                        int border_mode, cudaStream_t st) {
+  switch (s) {
+    case 1: launch_sep_pair<NC, 1>(src, dst, d, zt, w, border_mode, st); break;
+    case 2: launch_sep_pair<NC, 2>(src, dst, d, zt, w, border_mode, st); break;
+    case 3: launch_sep_pair<NC, 3>(src, dst, d, zt, w, border_mode, st); break;
+    case 4: launch_sep_pair<NC, 4>(src, dst, d, zt, w, border_mode, st); break;
+    case 5: launch_sep_pair<NC, 5>(src, dst, d, zt, w, border_mode, st); break;
+    default: launch_sep_pair<NC, 6>(src, dst, d, zt, w, border_mode, st); break;
+  }
+}
+
+void launch_gauss_sep_pair(const float *src, float *dst, Dims4 d, int nc, int zt, int s,
+                           const float *w1d, int border_mode, cudaStream_t st) {
+  W1 w;
+  for (int q = 0; q < 7; ++q) w.w[q] = q <= s ? w1d[q] : 0.f;
+  if (nc == 4) launch_sep_pair_nc<4>(src, dst, d, zt, s, w, border_mode, st);
+  else launch_sep_pair_nc<1>(src, dst, d, zt, s, w, border_mode, st);
 }
 
 // ---------------------------------------------------------------------------

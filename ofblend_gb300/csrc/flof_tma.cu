@@ -11,10 +11,12 @@
 // on an mbarrier, with NSTAGE slabs in flight.  For the extrapolation sweep
 // four output planes share every slab, which halves the L2-to-SM traffic
 // that bounds it.  The
-// tensor map views the float4 grid as a 5D float tensor (component, x, y, z,
-// t), so the innermost coordinate is always 0 (16-byte aligned) and cells
-// outside the grid arrive as zeros, which leave a running float sum
-// unchanged.  Lane l of a warp computes column x0+l for RY consecutive rows of
+// tensor map views the float4 grid as a 4D float tensor (4X, Y, Z, T), so a
+// slab row is one contiguous 16W-byte run, the innermost coordinate 4x is a
+// multiple of 16 bytes for every x, and cells outside the grid arrive as
+// zeros, which leave a running float sum unchanged (a 16-byte innermost box
+// dimension, one float4 per row, made the copies several times slower).
+// Lane l of a warp computes column x0+l for RY consecutive rows of
 // each plane, so each 8-lane shared-memory phase reads 128 contiguous bytes
 // of the dense TMA layout.
 //
@@ -89,9 +91,9 @@ __device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map,
                                               int z, int t, uint64_t *bar) {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
   asm volatile(
-      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(0), "r"(x), "r"(y), "r"(z), "r"(t), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(4 * x), "r"(y), "r"(z), "r"(t), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -422,6 +424,134 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
 }
 
+// The separable extrapolation sweep (blurType 2) walking t.  It takes
+// k_expol_tw's slabs in k_expol_tw's order but forms each output's 3^4 sum as
+// box sums: per slab the x sums of the rows a thread needs and the y sums of
+// three of those, added over the three z slabs of each output plane as the
+// slabs arrive, and over three consecutive t planes from a register ring.
+// Each sum is taken in the two-pass separable sweep's order (x, then y, z, t,
+// each (a-1 + a0) + a+1), so the two give the same bits; a cell costs about
+// fourteen float4 adds instead of 81, and RY = 4 rows per thread cut the
+// shared-memory reads per cell, which then bound the kernel.
+constexpr int ESW_RY = 4, ESW_NW = ETW_TY / ESW_RY, ESW_TC = 8, ESW_NS = 4, ESW_MINB = 3;
+constexpr int ESW_SMEM = ESW_NS * ETW_STRIDE;
+
+__global__ void __launch_bounds__(32 * ESW_NW, ESW_MINB)
+k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
+               int tiles_x, const uint16_t *__restrict__ fixed, int *err) {
+  extern __shared__ __align__(128) unsigned char raw[];
+  __shared__ __align__(8) uint64_t bar[ESW_NS];
+  constexpr int RY = ESW_RY, DZ = ETW_DZ, KZ = ETW_KZ, NS = ESW_NS;
+  constexpr int MRY = ExpolGeom::RY, DT = ExpolGeom::DT;  // keep-mask word geometry
+  static_assert(RY % MRY == 0, "a thread's rows cover whole keep-mask row groups");
+  static_assert((DT & (DT - 1)) == 0, "t % DT as a mask");
+  const int tile = blockIdx.x;
+  const int x0 = (tile % tiles_x) * TX, y0 = (tile / tiles_x) * ETW_TY;
+  const int z0 = blockIdx.y * DZ, t0 = blockIdx.z * ESW_TC;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int x = x0 + tx;
+  const int ygroups = (d.y + MRY - 1) / MRY, zgroups = (d.z + DZ - 1) / DZ;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int b = 0; b < NS; ++b) mbar_init(&bar[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
+  const int NP = (ESW_TC + 2) * KZ;  // slab p: plane t0 - 1 + p / KZ, z0 - 1 + p % KZ
+  auto issue = [&](int p) {
+    uint64_t *b = &bar[p % NS];
+    mbar_expect_tx(b, ETW_BYTES);
+    tma_load_slab(raw + (p % NS) * ETW_STRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + p % KZ,
+                  t0 - 1 + p / KZ, b);
+  };
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int p = 0; p < NS - 1; ++p) issue(p);
+  }
+  // z sums of planes tt - 2 (Z0), tt - 1 (Z1) and tt (Zc, filled slab by slab)
+  P4 Z0[DZ][RY], Z1[DZ][RY], Zc[DZ][RY];
+  for (int j = 0; j < ESW_TC + 2; ++j) {
+    // keep-mask words of output plane t = t0 - 2 + j, loaded before its slabs
+    // are summed (all ones: nothing to write)
+    const int t = t0 - 2 + j;
+    unsigned keep[RY / MRY];
+#pragma unroll
+    for (int g = 0; g < RY / MRY; ++g) {
+      const int yb = y0 + RY * ty + g * MRY;
+      keep[g] = 0xffffu;
+      if (j >= 2 && x < d.x && t < d.t && yb < d.y)
+        keep[g] = __ldg(fixed + ((((size_t)(t / DT) * zgroups + blockIdx.y) * ygroups + yb / MRY) *
+                                     d.x + x));
+    }
+#pragma unroll
+    for (int zk = 0; zk < KZ; ++zk) {
+      const int p = j * KZ + zk;
+      if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
+      const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
+          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
+        }
+        __syncthreads();
+        return;
+      }
+      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE) + RY * ty * ETW_W + tx;
+      auto xsum = [&](int k) {
+        const P4 *row = cur + k * ETW_W;
+        P4 v = row[0];
+        acc4(v, row[1]);
+        acc4(v, row[2]);
+        return v;
+      };
+      P4 r0 = xsum(0), r1 = xsum(1);
+#pragma unroll
+      for (int q = 0; q < RY; ++q) {
+        const P4 r2 = xsum(q + 2);
+        P4 xy = r0;
+        acc4(xy, r1);
+        acc4(xy, r2);
+#pragma unroll
+        for (int oz = 0; oz < DZ; ++oz) {
+          const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
+          if (zrel == -1) Zc[oz][q] = xy;
+          else if (zrel <= 1) acc4(Zc[oz][q], xy);
+        }
+        r0 = r1;
+        r1 = r2;
+      }
+      __syncthreads();
+    }
+    // output plane t: (Z(t - 1) + Z(t)) + Z(t + 1).  A clear bit means an
+    // unmarked interior cell, so x, y, z and t are then inside the grid.
+#pragma unroll
+    for (int g = 0; g < RY / MRY; ++g) {
+      const int yb = y0 + RY * ty + g * MRY;
+#pragma unroll
+      for (int oz = 0; oz < DZ; ++oz) {
+#pragma unroll
+        for (int m = 0; m < MRY; ++m) {
+          if (keep[g] >> ((oz * DT + (t & (DT - 1))) * MRY + m) & 1u) continue;
+          const int q = g * MRY + m;
+          P4 v = Z0[oz][q];
+          acc4(v, Z1[oz][q]);
+          acc4(v, Zc[oz][q]);
+          const float4 s = unpack4(v);
+          dst[d.index(x, yb + m, z0 + oz, t)] =
+              make_float4(mul_inv81(s.x), mul_inv81(s.y), mul_inv81(s.z), mul_inv81(s.w));
+        }
+      }
+    }
+#pragma unroll
+    for (int oz = 0; oz < DZ; ++oz)
+#pragma unroll
+      for (int q = 0; q < RY; ++q) {
+        Z0[oz][q] = Z1[oz][q];
+        Z1[oz][q] = Zc[oz][q];
+      }
+  }
+}
+
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -439,18 +569,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// Tensor map of a float4 grid as a 5D float tensor (4, X, Y, Z, T) with a
-// (4, W, H, 1, 1) box.
+// Tensor map of a float4 grid as a 4D float tensor (4X, Y, Z, T) with a
+// (4W, H, 1, 1) box: each slab row is one contiguous run of 16W bytes.
 bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
-  if (!fn || ((uintptr_t)base & 15)) return false;
-  const cuuint64_t dims[5] = {4, (cuuint64_t)d.x, (cuuint64_t)d.y, (cuuint64_t)d.z,
+  if (!fn || ((uintptr_t)base & 15) || 4 * W > 256) return false;
+  const cuuint64_t dims[4] = {(cuuint64_t)4 * d.x, (cuuint64_t)d.y, (cuuint64_t)d.z,
                               (cuuint64_t)d.t};
-  const cuuint64_t strides[4] = {16, (cuuint64_t)16 * d.x, (cuuint64_t)16 * d.x * d.y,
+  const cuuint64_t strides[3] = {(cuuint64_t)16 * d.x, (cuuint64_t)16 * d.x * d.y,
                                  (cuuint64_t)16 * d.x * d.y * d.z};
-  const cuuint32_t box[5] = {4, (cuuint32_t)W, (cuuint32_t)H, 1, 1};
-  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, (void *)base, dims, strides, box, es,
+  const cuuint32_t box[4] = {(cuuint32_t)(4 * W), (cuuint32_t)H, 1, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void *)base, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -556,6 +686,27 @@ bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 
   const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + ETW_TY - 1) / ETW_TY;
   dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
   k_expol_tw<<<grid, 32 * ETW_NW, ETW_SMEM, st>>>(map, out, d, tiles_x, mask, err);
+  return true;
+}
+
+bool launch_expol_sep_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 d, int *err,
+                         cudaStream_t st) {
+  const int zgroups = (d.z + ETW_DZ - 1) / ETW_DZ, tgroups = (d.t + ESW_TC - 1) / ESW_TC;
+  if (zgroups > 65535 || tgroups > 65535) return false;
+  CUtensorMap map;
+  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H)) return false;
+  static const bool attr = [] {
+    if (cudaFuncSetAttribute(k_expol_sep_tw, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             ESW_SMEM) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return true;
+  }();
+  if (!attr) return false;
+  const int tiles_x = (d.x + TX - 1) / TX, tiles_y = (d.y + ETW_TY - 1) / ETW_TY;
+  dim3 grid(tiles_x * tiles_y, zgroups, tgroups);
+  k_expol_sep_tw<<<grid, 32 * ESW_NW, ESW_SMEM, st>>>(map, out, d, tiles_x, mask, err);
   return true;
 }
 

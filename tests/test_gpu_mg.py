@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import ofblend_gb300 as F
-from ofblend_gb300 import synth
+from ofblend_gb300 import _lib, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -103,6 +103,23 @@ def test_separable_stencils_match_direct(case):
         print(f"{solver}: blurType 2 vs 1 rel L2 {rel_l2(b, a):.2e}, error metric {eb} vs {ea}")
         assert rel_l2(b, a) < 1e-4
         assert abs(eb - ea) <= 1e-3 * ea
+
+
+def test_slab_tma_kernels_match_plain_loads(case):
+    """The TMA slab kernels (the Vec4 blur and the extrapolation sweeps
+    walking t, direct and separable) and their plain-load counterparts take
+    the same sums in the same order: whole solves with the final projection
+    agree bit for bit, on an x extent that leaves a partial tile."""
+    kw = dict(FLOF, doFinalProject=True)
+    ctx = F.context()
+    for blur in (1, 2):
+        a, ea, _ = _solve(case, blurType=blur, **kw)
+        ctx.set_option(_lib.FLOF_OPT_SLAB_TMA, 0)
+        try:
+            b, eb, _ = _solve(case, blurType=blur, **kw)
+        finally:
+            ctx.set_option(_lib.FLOF_OPT_SLAB_TMA, 1)
+        assert np.array_equal(a, b) and ea == eb, (blur, rel_l2(b, a), ea, eb)
 
 
 def test_mg_params_are_checked(gpu):
