@@ -11,6 +11,8 @@
 //   knCvExpolBlur4d        :613-626
 #include <float.h>
 
+#include <algorithm>
+
 #include "flof_kernels.h"
 
 namespace flof {
@@ -778,8 +780,33 @@ __device__ __forceinline__ float4 sep_ring(const W1 &w, const float4 (&r)[2 * S 
 }
 
 constexpr int SEP_RUN = 16;  // y rows or t planes walked per thread
+constexpr int SEP_ZB = 8;    // z planes per block of the z-t kernel (32 x 8 threads)
+static_assert(32 * SEP_ZB == NT, "the z-t kernel's block is NT threads");
 
-// dst(x, y, z, t) = the y sum of the x sums, every cell
+// The 2S + 1 taps of an axis sum around cell `id` with stride `step`; taps
+// outside the axis (c + o out of 0..n-1) or a cell outside the walk
+// (live == false) read as zero and are never used.
+template <int NC, int S>
+__device__ __forceinline__ void load_taps(float4 (&a)[2 * S + 1], const float *src, idx_t id,
+                                          idx_t step, int c, int n, bool live) {
+#pragma unroll
+  for (int o = -S; o <= S; ++o)
+    a[o + S] = (live && c + o >= 0 && c + o < n) ? ld_nc<NC>(src, id + o * step)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+template <int S>
+__device__ __forceinline__ float4 sum_taps(const W1 &w, const float4 (&a)[2 * S + 1], int c, int n,
+                                           float inv) {
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int o = -S; o <= S; ++o)
+    if (c + o >= 0 && c + o < n) fma4(v, w.w[o < 0 ? -o : o], a[o + S]);
+  return scale4(v, inv);
+}
+
+// dst(x, y, z, t) = the y sum of the x sums, every cell.  A thread walks a
+// run of y rows; the taps of the next row are loaded before the current
+// row's sums are formed.
 template <int NC, int S>
 __global__ void __launch_bounds__(NT)
 k_blur_sep_xy(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W1 w,
@@ -794,41 +821,49 @@ k_blur_sep_xy(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W
     const int ya = (int)(r / (uint32_t)d.t) * SEP_RUN, yb = min(ya + SEP_RUN, d.y);
     const idx_t plane = d.index(x, 0, z, t);
     const float ix = sep_inv<S>(w, x, d.x);
-    auto xsum = [&](int y) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (y < 0 || y >= d.y) return v;  // out of range: never used
-      const idx_t id = plane + y * sY;
+    float4 ring[2 * S + 1], a[2 * S + 1];
 #pragma unroll
-      for (int o = -S; o <= S; ++o)
-        if (x + o >= 0 && x + o < d.x) fma4(v, w.w[o < 0 ? -o : o], ld_nc<NC>(src, id + o));
-      return scale4(v, ix);
-    };
-    float4 ring[2 * S + 1];
-#pragma unroll
-    for (int k = 1; k <= 2 * S; ++k) ring[k] = xsum(ya - S - 1 + k);
+    for (int k = 1; k <= 2 * S; ++k) {
+      const int y = ya - S - 1 + k;
+      const bool live = y >= 0 && y < d.y;
+      load_taps<NC, S>(a, src, plane + y * sY, 1, x, d.x, live);
+      ring[k] = sum_taps<S>(w, a, x, d.x, ix);
+    }
+    load_taps<NC, S>(a, src, plane + (ya + S) * sY, 1, x, d.x, ya + S < d.y);
     for (int y = ya; y < yb; ++y) {
+      float4 cur[2 * S + 1];
+#pragma unroll
+      for (int k = 0; k <= 2 * S; ++k) cur[k] = a[k];
+      load_taps<NC, S>(a, src, plane + (y + S + 1) * sY, 1, x, d.x, y + 1 < yb && y + S + 1 < d.y);
 #pragma unroll
       for (int k = 0; k < 2 * S; ++k) ring[k] = ring[k + 1];
-      ring[2 * S] = xsum(y + S);
+      ring[2 * S] = sum_taps<S>(w, cur, x, d.x, ix);
       st_nc<NC>(dst, plane + y * sY, sep_ring<S>(w, ring, y, d.y));
     }
   }
 }
 
 // dst(x, y, z, t) = the t sum of the z sums at interior cells; border_mode 1
-// writes zeros on the one-cell ring, 2 leaves it alone
+// writes zeros on the one-cell ring, 2 leaves it alone.  A block is 32 x
+// columns by SEP_ZB z planes at one y, so the z taps of a thread are mostly
+// its neighbours' cells, read through L1; each thread walks a run of t
+// planes, loading the next plane's taps before the current sums are formed.
 template <int NC, int S>
 __global__ void __launch_bounds__(NT)
 k_blur_sep_zt(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W1 w,
-              int border_mode, uint32_t n) {
+              int border_mode, int xtiles, int ztiles, uint32_t nblocks) {
   const idx_t sZ = d.sz(), sT = d.st();
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int x = (int)(q % (uint32_t)d.x);
-    uint32_t r = q / (uint32_t)d.x;
+  const int tx = threadIdx.x & 31, tz = threadIdx.x >> 5;
+  for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    uint32_t r = b;
+    const int xt = (int)(r % (uint32_t)xtiles);
+    r /= (uint32_t)xtiles;
     const int y = (int)(r % (uint32_t)d.y);
     r /= (uint32_t)d.y;
-    const int z = (int)(r % (uint32_t)d.z);
-    const int ta = (int)(r / (uint32_t)d.z) * SEP_RUN, tb = min(ta + SEP_RUN, d.t);
+    const int zt = (int)(r % (uint32_t)ztiles);
+    const int ta = (int)(r / (uint32_t)ztiles) * SEP_RUN, tb = min(ta + SEP_RUN, d.t);
+    const int x = xt * 32 + tx, z = zt * SEP_ZB + tz;
+    if (x >= d.x || z >= d.z) continue;
     const idx_t col = d.index(x, y, z, 0);
     const bool ring_xyz = x < 1 || x >= d.x - 1 || y < 1 || y >= d.y - 1 || z < 1 || z >= d.z - 1;
     if (ring_xyz) {
@@ -837,22 +872,22 @@ k_blur_sep_zt(const float *__restrict__ src, float *__restrict__ dst, Dims4 d, W
       continue;
     }
     const float iz = sep_inv<S>(w, z, d.z);
-    auto zsum = [&](int t) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (t < 0 || t >= d.t) return v;  // out of range: never used
-      const idx_t id = col + t * sT;
+    float4 ring[2 * S + 1], a[2 * S + 1];
 #pragma unroll
-      for (int o = -S; o <= S; ++o)
-        if (z + o >= 0 && z + o < d.z) fma4(v, w.w[o < 0 ? -o : o], ld_nc<NC>(src, id + o * sZ));
-      return scale4(v, iz);
-    };
-    float4 ring[2 * S + 1];
-#pragma unroll
-    for (int k = 1; k <= 2 * S; ++k) ring[k] = zsum(ta - S - 1 + k);
+    for (int k = 1; k <= 2 * S; ++k) {
+      const int t = ta - S - 1 + k;
+      load_taps<NC, S>(a, src, col + t * sT, sZ, z, d.z, t >= 0 && t < d.t);
+      ring[k] = sum_taps<S>(w, a, z, d.z, iz);
+    }
+    load_taps<NC, S>(a, src, col + (ta + S) * sT, sZ, z, d.z, ta + S < d.t);
     for (int t = ta; t < tb; ++t) {
+      float4 cur[2 * S + 1];
+#pragma unroll
+      for (int k = 0; k <= 2 * S; ++k) cur[k] = a[k];
+      load_taps<NC, S>(a, src, col + (t + S + 1) * sT, sZ, z, d.z, t + 1 < tb && t + S + 1 < d.t);
 #pragma unroll
       for (int k = 0; k < 2 * S; ++k) ring[k] = ring[k + 1];
-      ring[2 * S] = zsum(t + S);
+      ring[2 * S] = sum_taps<S>(w, cur, z, d.z, iz);
       if (t < 1 || t >= d.t - 1) {
         if (border_mode == 1) st_nc<NC>(dst, col + t * sT, make_float4(0.f, 0.f, 0.f, 0.f));
         continue;
@@ -869,8 +904,12 @@ void launch_sep_pair(const float *src, float *dst, Dims4 d, int zt, const W1 &w,
     const uint32_t n = (uint32_t)((long long)d.x * d.z * d.t * ((d.y + SEP_RUN - 1) / SEP_RUN));
     k_blur_sep_xy<NC, S><<<grid_for(n, NT, 8), NT, 0, st>>>(src, dst, d, w, n);
   } else {
-    const uint32_t n = (uint32_t)((long long)d.x * d.y * d.z * ((d.t + SEP_RUN - 1) / SEP_RUN));
-    k_blur_sep_zt<NC, S><<<grid_for(n, NT, 8), NT, 0, st>>>(src, dst, d, w, border_mode, n);
+    const int xtiles = (d.x + 31) / 32, ztiles = (d.z + SEP_ZB - 1) / SEP_ZB;
+    const uint32_t nb =
+        (uint32_t)((long long)xtiles * d.y * ztiles * ((d.t + SEP_RUN - 1) / SEP_RUN));
+    const int grid = (int)std::min<long long>(nb, (long long)sm_count() * 8);
+    k_blur_sep_zt<NC, S><<<grid, 32 * SEP_ZB, 0, st>>>(src, dst, d, w, border_mode, xtiles, ztiles,
+                                                       nb);
   }
 }
 template <int NC>

@@ -431,9 +431,13 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
 // slabs arrive, and over three consecutive t planes from a register ring.
 // Each sum is taken in the two-pass separable sweep's order (x, then y, z, t,
 // each (a-1 + a0) + a+1), so the two give the same bits; a cell costs about
-// fourteen float4 adds instead of 81, and RY = 4 rows per thread cut the
-// shared-memory reads per cell, which then bound the kernel.
-constexpr int ESW_RY = 4, ESW_NW = ETW_TY / ESW_RY, ESW_TC = 8, ESW_NS = 4, ESW_MINB = 3;
+// sixteen float4 adds instead of 81.  The kernel is bound by latency (few
+// warps, two dependent shared-memory and add steps per slab) more than by
+// shared-memory or DRAM bandwidth, so warps count most: at 64^4 on GB300,
+// RY = 2 rows per thread (8 warps, three blocks per SM) took 0.168 ms a
+// sweep against 0.178 ms for RY = 4 (4 warps), and TC = 4 or deeper slab
+// pipelines did not help.
+constexpr int ESW_RY = 2, ESW_NW = ETW_TY / ESW_RY, ESW_TC = 8, ESW_NS = 4, ESW_MINB = 3;
 constexpr int ESW_SMEM = ESW_NS * ETW_STRIDE;
 
 __global__ void __launch_bounds__(32 * ESW_NW, ESW_MINB)
@@ -487,15 +491,9 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
     for (int zk = 0; zk < KZ; ++zk) {
       const int p = j * KZ + zk;
       if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
+      // A thread whose wait gave up still reads the buffer (stale values,
+      // in bounds); the barrier that ends the slab's step then ends the block.
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
-      if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) {
-          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
-          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
-        }
-        __syncthreads();
-        return;
-      }
       const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE) + RY * ty * ETW_W + tx;
       auto xsum = [&](int k) {
         const P4 *row = cur + k * ETW_W;
@@ -520,7 +518,14 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
         r0 = r1;
         r1 = r2;
       }
-      __syncthreads();
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
+          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
+        }
+        __syncthreads();
+        return;
+      }
     }
     // output plane t: (Z(t - 1) + Z(t)) + Z(t + 1).  A clear bit means an
     // unmarked interior cell, so x, y, z and t are then inside the grid.
