@@ -340,32 +340,25 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
   // running sums of outputs tt - 1 (A), tt (B) and tt + 1 (C)
   P4 A[DZ][RY], B[DZ][RY], C[DZ][RY];
+  // One t plane j (tt = t0 - 1 + j).  SA, SB, SC say which of the three
+  // outputs lie in the block's range t0 .. t0 + ETW_TC - 1: the first two and
+  // the last two planes skip the sums of the others (a fifth of the adds).
+  auto plane = [&](int j, auto SA, auto SB, auto SC) -> bool {
+    constexpr bool DA = decltype(SA)::value, DB = decltype(SB)::value, DC = decltype(SC)::value;
+    if (DC) {
 #pragma unroll
-  for (int oz = 0; oz < DZ; ++oz)
+      for (int oz = 0; oz < DZ; ++oz)
 #pragma unroll
-    for (int q = 0; q < RY; ++q) {
-      memset(&A[oz][q], 0, sizeof(P4));
-      memset(&B[oz][q], 0, sizeof(P4));
+        for (int q = 0; q < RY; ++q) memset(&C[oz][q], 0, sizeof(P4));
     }
-  for (int j = 0; j < ETW_TC + 2; ++j) {
-#pragma unroll
-    for (int oz = 0; oz < DZ; ++oz)
-#pragma unroll
-      for (int q = 0; q < RY; ++q) memset(&C[oz][q], 0, sizeof(P4));
 #pragma unroll
     for (int zk = 0; zk < KZ; ++zk) {
       const int p = j * KZ + zk;
       // buffer (p - 1) % NS was released by the barrier that ended slab p - 1
       if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
+      // A thread whose wait gave up still reads the buffer (stale values, in
+      // bounds); the barrier that ends the slab's step then ends the block.
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
-      if (__syncthreads_or(!ok)) {
-        if (threadIdx.x == 0) {
-          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
-          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
-        }
-        __syncthreads();
-        return;
-      }
       const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE);
 #pragma unroll
       for (int k = 0; k < RY + 2; ++k) {
@@ -380,23 +373,36 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
             const int yj = k - q - 1;
             if (yj < -1 || yj > 1) continue;
             // vt = -1 of output tt + 1, vt = 0 of output tt, vt = +1 of output tt - 1
-            acc4(C[oz][q], a0);
-            acc4(C[oz][q], a1);
-            acc4(C[oz][q], a2);
-            acc4(B[oz][q], a0);
-            acc4(B[oz][q], a1);
-            acc4(B[oz][q], a2);
-            acc4(A[oz][q], a0);
-            acc4(A[oz][q], a1);
-            acc4(A[oz][q], a2);
+            if (DC) {
+              acc4(C[oz][q], a0);
+              acc4(C[oz][q], a1);
+              acc4(C[oz][q], a2);
+            }
+            if (DB) {
+              acc4(B[oz][q], a0);
+              acc4(B[oz][q], a1);
+              acc4(B[oz][q], a2);
+            }
+            if (DA) {
+              acc4(A[oz][q], a0);
+              acc4(A[oz][q], a1);
+              acc4(A[oz][q], a2);
+            }
           }
         }
       }
-      __syncthreads();
+      if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+          atomicExch(err, FLOF_DEV_ERR_TMA_TIMEOUT);
+          for (int r = p; r < NP && r < p + NS; ++r) mbar_wait_bounded(&bar[r % NS], (r / NS) & 1);
+        }
+        __syncthreads();
+        return false;
+      }
     }
     // output tt - 1 = t0 - 2 + j is complete
     const int t = t0 - 2 + j;
-    if (j >= 2 && xy_ok && t < d.t) {
+    if (DA && xy_ok && t < d.t) {
       const unsigned keep =
           __ldg(fixed + (((size_t)(t / DT) * zgroups + blockIdx.y) * ygroups + yg) * d.x + x);
 #pragma unroll
@@ -421,7 +427,17 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
         A[oz][q] = B[oz][q];
         B[oz][q] = C[oz][q];
       }
-  }
+    return true;
+  };
+  using T_ = std::true_type;
+  using F_ = std::false_type;
+  static_assert(ETW_TC >= 2, "the peeled planes are distinct");
+  if (!plane(0, F_(), F_(), T_())) return;
+  if (!plane(1, F_(), T_(), T_())) return;
+  for (int j = 2; j < ETW_TC; ++j)
+    if (!plane(j, T_(), T_(), T_())) return;
+  if (!plane(ETW_TC, T_(), T_(), F_())) return;
+  plane(ETW_TC + 1, T_(), F_(), F_());
 }
 
 // The separable extrapolation sweep (blurType 2) walking t.  It takes
