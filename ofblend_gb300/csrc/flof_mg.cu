@@ -303,6 +303,23 @@ k_mg0_prolong(float4 *__restrict__ x, const float4 *__restrict__ e1, Dims4 d, Bo
 // t neighbours cost no load); z . b for the PCG: init sets sigma (and
 // beta = 0), otherwise beta = z.b / sigma and sigma = z.b.
 constexpr int MG_TT = 8;
+struct PostLoads {
+  float4 yp, zm, ym, xm, xp, yq, zp, gg, bb;
+};
+__device__ __forceinline__ void post_load(PostLoads &a, const float4 *__restrict__ b,
+                                          const float4 *__restrict__ g,
+                                          const float4 *__restrict__ y, idx_t id, idx_t sY,
+                                          idx_t sZ, idx_t sT) {
+  a.yp = __ldg(y + id + sT);
+  a.zm = __ldg(y + id - sZ);
+  a.ym = __ldg(y + id - sY);
+  a.xm = __ldg(y + id - 1);
+  a.xp = __ldg(y + id + 1);
+  a.yq = __ldg(y + id + sY);
+  a.zp = __ldg(y + id + sZ);
+  a.gg = __ldg(g + id);
+  a.bb = __ldg(b + id);
+}
 __global__ void __launch_bounds__(MT)
 k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
               const float4 *__restrict__ y, float4 *__restrict__ z, Dims4 d, BoxDecoder bxyz,
@@ -372,44 +389,71 @@ k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
   }
 }
 
-// The level-0 residual with the restriction folded in: a block is 8 warps;
-// warp w covers the 32 interior cells x = 1 + 32 bx .. 32 + 32 bx of row
-// (y, z, t) = 1 + 2 (by, bz, bt) + (w & 1, (w >> 1) & 1, w >> 2), so the
-// block holds 16 whole aggregates.  Lanes 2a and 2a+1 add their residuals,
-// then the 8 warps' pair sums are added in warp order: b1 of the 16
-// aggregates, with no level-0 residual written.
-__global__ void __launch_bounds__(MT)
+// The level-0 residual with the restriction folded in, walking t.  A block
+// is 4 warps: warp w covers the 32 interior cells x = 1 + 32 bx .. 32 + 32 bx
+// of the row (y, z) = 1 + 2 (by, bz) + (w & 1, w >> 1) and walks the RR_TP
+// aggregate t pairs of its chunk, with x at t-1, t and t+1 in registers (the
+// t neighbours cost no load).  For each t pair, lanes 2a and 2a+1 add their
+// residuals; then each of the 16 aggregates adds the 4 warps' pair sums of
+// the pair's first plane and then of its second, in warp order: b1 of the 16
+// aggregates, with no level-0 residual written.  The sums and their order
+// are those of one cell per thread with warp (y & 1) + 2 (z & 1) + 4 (t & 1).
+constexpr int RR_NT = 128, RR_TP = 4;
+__global__ void __launch_bounds__(RR_NT)
 k_mg0_resid_restrict(const float4 *__restrict__ b, const float4 *__restrict__ g,
                      const float4 *__restrict__ x, float4 *__restrict__ b1, Dims4 d, Dims4 m,
                      int nbx, float c0, float wS, const CGState *st) {
   pdl_wait();
   pdl_launch_dependents();
   if (mg_stop(st)) return;
-  __shared__ float4 part[8][16];
+  __shared__ float4 part[2][2][4][16];  // [pair parity][plane of the pair][warp][aggregate]
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int bxi = blockIdx.x % nbx, rest = blockIdx.x / nbx;
   const int by = rest % m.y, rest2 = rest / m.y;
-  const int bz = rest2 % m.z, bt = rest2 / m.z;
-  const int i = 1 + 32 * bxi + lane;
-  const int j = 1 + 2 * by + (w & 1), k = 1 + 2 * bz + ((w >> 1) & 1), l = 1 + 2 * bt + (w >> 2);
-  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i <= d.x - 2 && j <= d.y - 2 && k <= d.z - 2 && l <= d.t - 2) {
-    const idx_t id = d.index(i, j, k, l);
-    r = f4_sub(__ldg(b + id), a0_mul(x, __ldg(g + id), id, d.x, d.sz(), d.st(), c0, wS));
-  }
-  r.x += __shfl_down_sync(0xffffffffu, r.x, 1);
-  r.y += __shfl_down_sync(0xffffffffu, r.y, 1);
-  r.z += __shfl_down_sync(0xffffffffu, r.z, 1);
-  r.w += __shfl_down_sync(0xffffffffu, r.w, 1);
-  if ((lane & 1) == 0) part[w][lane >> 1] = r;
-  __syncthreads();
-  if (threadIdx.x < 16) {
-    const int K0 = 16 * bxi + threadIdx.x;
-    if (K0 < m.x) {
-      float4 s = part[0][threadIdx.x];
+  const int bz = rest2 % m.z, btc = rest2 / m.z;
+  const int i = 1 + 32 * bxi + lane, j = 1 + 2 * by + (w & 1), k = 1 + 2 * bz + (w >> 1);
+  const bool live = i <= d.x - 2 && j <= d.y - 2 && k <= d.z - 2;
+  const int bt0 = btc * RR_TP, bt1 = min(bt0 + RR_TP, m.t);
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  // border cells of x hold zero, so the neighbour loads need no guards
+  idx_t id = live ? d.index(i, j, k, 1 + 2 * bt0) : 0;
+  float4 xm = live ? __ldg(x + id - sT) : zero4, xc = live ? __ldg(x + id) : zero4;
+  for (int bt = bt0; bt < bt1; ++bt) {
+    float4 r[2];
 #pragma unroll
-      for (int q = 1; q < 8; ++q) s = f4_add(s, part[q][threadIdx.x]);
-      b1[m.index(K0, by, bz, bt)] = s;
+    for (int h = 0; h < 2; ++h) {
+      r[h] = zero4;
+      if (live && 1 + 2 * bt + h <= d.t - 2) {
+        const float4 xp = __ldg(x + id + sT);
+        float4 nb = f4_add(xm, __ldg(x + id - sZ));
+        nb = f4_add(nb, __ldg(x + id - sY));
+        nb = f4_add(nb, __ldg(x + id - 1));
+        nb = f4_add(nb, __ldg(x + id + 1));
+        nb = f4_add(nb, __ldg(x + id + sY));
+        nb = f4_add(nb, __ldg(x + id + sZ));
+        nb = f4_add(nb, xp);
+        r[h] = f4_sub(__ldg(b + id), f4_axpy(-wS, nb, blk0_mul(__ldg(g + id), c0, xc)));
+        xm = xc;
+        xc = xp;
+        id += sT;
+      }
+      r[h].x += __shfl_down_sync(0xffffffffu, r[h].x, 1);
+      r[h].y += __shfl_down_sync(0xffffffffu, r[h].y, 1);
+      r[h].z += __shfl_down_sync(0xffffffffu, r[h].z, 1);
+      r[h].w += __shfl_down_sync(0xffffffffu, r[h].w, 1);
+      if ((lane & 1) == 0) part[bt & 1][h][w][lane >> 1] = r[h];
+    }
+    // part[bt & 1] was last read before the barrier of pair bt - 1
+    __syncthreads();
+    if (threadIdx.x < 16) {
+      const int K0 = 16 * bxi + threadIdx.x;
+      if (K0 < m.x) {
+        float4 s = part[bt & 1][0][0][threadIdx.x];
+#pragma unroll
+        for (int q = 1; q < 8; ++q) s = f4_add(s, part[bt & 1][q >> 2][q & 3][threadIdx.x]);
+        b1[m.index(K0, by, bz, bt)] = s;
+      }
     }
   }
 }
@@ -855,9 +899,10 @@ void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0,
   }
   {
     const int nbx = (d.x - 2 + 31) / 32;
-    const long long nblk = (long long)nbx * L[0].m.y * L[0].m.z * L[0].m.t;
-    mg_launch(k_mg0_resid_restrict, (unsigned)nblk, MT, s, b0, g, x0, L[0].b, d, L[0].m, nbx, c0,
-              wS, st);
+    const int tchunks = (L[0].m.t + RR_TP - 1) / RR_TP;
+    const long long nblk = (long long)nbx * L[0].m.y * L[0].m.z * tchunks;
+    mg_launch(k_mg0_resid_restrict, (unsigned)nblk, RR_NT, s, b0, g, x0, L[0].b, d, L[0].m, nbx,
+              c0, wS, st);
     ++nl_;
   }
   for (int l = 0; l + 1 < nl; ++l) {
