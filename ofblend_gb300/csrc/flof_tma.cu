@@ -29,13 +29,13 @@
 #include <type_traits>
 
 #include "flof_kernels.h"
+#include "flof_tma.cuh"
 
 namespace flof {
 
 namespace {
 
 constexpr int TX = 32;                // tile width: one column per lane
-constexpr int WAIT_LIMIT = 1 << 22;   // try_wait polls before giving up
 
 // Tile geometry: NW warps, RY rows per thread, DT consecutive t planes and DZ
 // consecutive z planes per block, NSTAGE slab buffers in flight.
@@ -56,46 +56,6 @@ struct TG {
 // planes share every slab (24 slabs per 8 output planes), four in flight.
 template <int S> using BlurGeom = TG<S, 4, 8, 1, 1, 2>;
 using ExpolGeom = TG<1, 8, 2, 4, 2, 4, 3>;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  for (int i = 0; i < WAIT_LIMIT; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-// The slab buffers are reused: a copy lands (async proxy) in a buffer the
-// block's threads read before (generic proxy).  The issuing thread passes the
-// barrier that ends those reads and then fences the two proxies, so that no
-// read still in flight sees the new slab.
-__device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map, int x, int y,
-                                              int z, int t, uint64_t *bar) {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(4 * x), "r"(y), "r"(z), "r"(t), "r"(smem_u32(bar))
-      : "memory");
-}
 
 // The extrapolation sweep adds with sm_100-family packed `add.rn.f32x2`: a
 // float4 is two float pairs (x,y), (z,w), each lane rounded like the scalar
@@ -590,6 +550,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+}  // namespace
+
 // Tensor map of a float4 grid as a 4D float tensor (4X, Y, Z, T) with a
 // (4W, H, 1, 1) box: each slab row is one contiguous run of 16W bytes.
 bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) {
@@ -605,6 +567,8 @@ bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) 
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+namespace {
 
 template <int S, class G>
 bool launch_blur(const float4 *src, float4 *dst, Dims4 d, const float *wsum, const float *w,
