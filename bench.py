@@ -597,6 +597,7 @@ def run_gpu(a):
         rates_before = copy_rates()
         W.step_e2e(pinned, sink, ctx)
         torch.cuda.synchronize()
+        rates_warm = copy_rates()
         barrier(world)
         per = []
         t0 = time.perf_counter()
@@ -611,8 +612,10 @@ def run_gpu(a):
         rates_after = copy_rates()
         e2e_extra = {"ms_per_step": round(e2e_s * 1e3 / a.e2e_steps, 3),
                      "ms_per_step_min": round(min(per) * 1e3, 3),
+                     "ms_each": [round(t * 1e3, 1) for t in per],
                      "h2d_GBps": rates_after[0], "d2h_GBps": rates_after[1],
-                     "h2d_d2h_GBps_before": list(rates_before)}
+                     "h2d_d2h_GBps_before": list(rates_before),
+                     "h2d_d2h_GBps_after_warmup_step": list(rates_warm)}
 
     st = list(W.stats)
     iters = [s["solves"] for s in st]
