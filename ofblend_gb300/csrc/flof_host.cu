@@ -588,6 +588,8 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
     fail(FLOF_E_ARG, "postVelBlur must be finite");
   DBuf marker(c, real_bytes(d)), tmp(c, vec_bytes(d));
   DBuf mask(c, expol_mask_words(d) * sizeof(uint16_t));
+  // the projection's queue of cells that need a search, and its two counters
+  DBuf pqueue(c, project_queue_bytes(d)), pcount(c, 2 * sizeof(unsigned int));
   DBuf s2;  // the separable sweep's (x,y) box sums (blurType 2)
   int singleStep = 0;
   if (postVelBlur < blurThreshold) singleStep = 1;
@@ -597,9 +599,10 @@ void corr_vels_of(flof_ctx *c, Dims4 d, float4 *dst, float4 *vel, const float *p
     float4 *B = tmp.v();
     CK(cudaMemsetAsync(dst, 0, vec_bytes(d), c->stream));
     CK(cudaMemsetAsync(marker.p, 0, real_bytes(d), c->stream));
+    CK(cudaMemsetAsync(pcount.p, 0, 2 * sizeof(unsigned int), c->stream));
     KLP(c, KC_PROJECT, d.x, d.cells() * 44,
         launch_project_cells(dst, vel, phiOrg, phiTarget, marker.f(), d, threshPhi, maxIter,
-                               c->stream));
+                             pqueue.p, (unsigned int *)pcount.p, c->stream));
     if (doCvExtrapol > 0) {
       // The sweeps only rewrite unmarked interior cells; both buffers carry
       // the projected values everywhere else (the reference's tmp copy).

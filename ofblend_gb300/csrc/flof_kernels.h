@@ -308,9 +308,15 @@ bool launch_expol_sep_tw(const float4 *in, float4 *out, const uint16_t *mask, Di
                          cudaStream_t st);
 
 // ---- projection correction ------------------------------------------------------
+// knProjectCells in two kernels: the normals and the cells that finish
+// without a search, then the searches of the others, taken from `queue`
+// (project_queue_bytes(d) bytes) by whichever lane is free.  `counters` is
+// two unsigned ints, zero on entry.
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,
-                          float threshPhi, int maxIter, cudaStream_t s);
+                          float threshPhi, int maxIter, void *queue, unsigned int *counters,
+                          cudaStream_t s);
+size_t project_queue_bytes(Dims4 d);
 // one knCvExpolBlur4d sweep fused with the copy: out = unmarked interior ?
 // avg81(in) : in
 void launch_expol_sweep(const float4 *in, float4 *out, const float *mark,

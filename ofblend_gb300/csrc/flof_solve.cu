@@ -1006,14 +1006,44 @@ __device__ __forceinline__ float shifted_sample(const float *__restrict__ phi, c
   return ip16(S, D == 0 ? s : a[0], D == 1 ? s : a[1], D == 2 ? s : a[2], D == 3 ? s : a[3]);
 }
 
+// The state of a cell whose projection search is still to run.
+struct ProjState {
+  float4 p;    // the advected position
+  float4 nrm;  // the normalised normal
+  float dd, target;
+  uint32_t id, pad;
+};
+
+// The outcome of a cell's projection (optflow4d.cpp:725-732).
+__device__ __forceinline__ void project_write(float4 *__restrict__ dst, float *__restrict__ marker,
+                                              idx_t id, float4 nrm, float dd, float threshPhi) {
+  if (fabsf(dd) > threshPhi) {
+    dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  dst[id] = make_float4(nrm.x * dd, nrm.y * dd, nrm.z * dd, nrm.w * dd);
+  marker[id] = 1.f;
+}
+
+// knProjectCells, first part: per box cell the advected position, the normal
+// and the start of the search.  Cells with a zero normal (flat, clamped phi)
+// finish here; the others are appended to `queue` (warp-aggregated, in no
+// fixed order) for k_project_search.
 __global__ void __launch_bounds__(128)
-k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
-                const float *__restrict__ phiOrg, const float *__restrict__ phiTarget,
-                float *__restrict__ marker, Dims4 d, BoxDecoder bx, uint32_t nbox,
-                float threshPhi, int maxIter) {
+k_project_prep(float4 *__restrict__ dst, const float4 *__restrict__ vel,
+               const float *__restrict__ phiOrg, const float *__restrict__ phiTarget,
+               float *__restrict__ marker, Dims4 d, BoxDecoder bx, uint32_t nbox,
+               float threshPhi, int maxIter, ProjState *__restrict__ queue,
+               unsigned int *__restrict__ qcount) {
   const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nbox;
-       q += gridDim.x * blockDim.x) {
+  // every lane of a warp runs the same trip count, for the warp-wide append
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t trips = (nbox + stride - 1) / stride;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint32_t it = 0, q = blockIdx.x * blockDim.x + threadIdx.x; it < trips; ++it, q += stride) {
+    bool search = false;
+    ProjState S;
+    if (q < nbox) {
     int i, j, k, l;
     bx.decode(q, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
@@ -1062,12 +1092,9 @@ k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
     // projectCell (optflow4d.cpp:675-710)
     float step = 0.25f;
     if (maxIter < 50) step = 0.5f;
-    int lastDir = 0;
     const float targetVal = __ldg(phiTarget + id);
-    float vn = ip16(T, a[0], a[1], a[2], a[3]);
-    idx_t ti = ic;  // T holds the taps of the cell at ti
+    const float vn = ip16(T, a[0], a[1], a[2], a[3]);
     float dd = (vn - targetVal);
-    int lim = maxIter;
     if (nrm.x == 0.f && nrm.y == 0.f && nrm.z == 0.f && nrm.w == 0.f && isfinite(dd)) {
       // Zero normal (flat, clamped phi): every probe is p itself (p + 0 * dd),
       // so vn and the in-bounds test never change, the direction never flips,
@@ -1081,18 +1108,92 @@ k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
           for (int s = 0; s < maxIter; ++s) dd -= step;
         }
       }
-      lim = 0;
+      project_write(dst, marker, id, nrm, dd, threshPhi);
+    } else if (maxIter <= 0) {
+      project_write(dst, marker, id, nrm, dd, threshPhi);
+    } else {
+      search = true;
+      S.p = make_float4(p0, p1, p2, p3);
+      S.nrm = nrm;
+      S.dd = dd;
+      S.target = targetVal;
+      S.id = (uint32_t)id;
+      S.pad = 0;
     }
-    for (int s = 0; s < lim; ++s) {
-      const float n0 = p0 + (nrm.x * dd) * dt;
-      const float n1 = p1 + (nrm.y * dd) * dt;
-      const float n2 = p2 + (nrm.z * dd) * dt;
-      const float n3 = p3 + (nrm.w * dd) * dt;
-      if (!in_bounds(d, trunc_i(n0), trunc_i(n1), trunc_i(n2), trunc_i(n3), 0)) {
-        s = lim;
-        dd = 9999.f;
-        continue;
+    }
+    const unsigned want = __ballot_sync(0xffffffffu, search);
+    if (want) {
+      unsigned base = 0;
+      if (lane == (unsigned)(__ffs(want) - 1)) base = atomicAdd(qcount, (unsigned)__popc(want));
+      base = __shfl_sync(0xffffffffu, base, __ffs(want) - 1);
+      if (search) queue[base + __popc(want & ((1u << lane) - 1u))] = S;
+    }
+  }
+}
+
+// knProjectCells, the search (projectCell, optflow4d.cpp:675-710) of the
+// queued cells.  A lane pulls its next cell when its search ends, so the
+// lanes of a warp stay busy whatever the cells' step counts (1 to maxIter).
+// Warps take chunks of PROJ_CHUNK queue entries; within a chunk the lanes
+// that need a cell take consecutive entries in lane order.  Every cell's
+// arithmetic is the single-cell search's, so the results do not depend on
+// which lane runs a cell.
+constexpr int PROJ_CHUNK = 256;
+__global__ void __launch_bounds__(128)
+k_project_search(float4 *__restrict__ dst, const float *__restrict__ phiOrg,
+                 float *__restrict__ marker, Dims4 d, float threshPhi, int maxIter,
+                 const ProjState *__restrict__ queue, const unsigned int *__restrict__ qcount,
+                 unsigned int *__restrict__ qhead) {
+  const idx_t sY = d.x, sZ = d.sz(), sT = d.st();
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned n = *qcount;
+  const float dt = 1.0f;
+  unsigned next = 0, end = 0;  // the warp's current chunk
+  bool drained = false;        // the queue has no chunk left for this warp
+  bool active = false;
+  ProjState S;
+  float T[16];
+  idx_t ti = -1;
+  float step = 0.f;
+  int lastDir = 0, s = 0;
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active);
+    while (need && !drained) {
+      if (next >= end) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(qhead, (unsigned)PROJ_CHUNK);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) {
+          drained = true;
+          break;
+        }
+        next = base;
+        end = min(base + (unsigned)PROJ_CHUNK, n);
       }
+      const unsigned k = next + __popc(need & ((1u << lane) - 1u));
+      if (!active && k < end) {
+        S = queue[k];
+        active = true;
+        ti = -1;
+        step = maxIter < 50 ? 0.5f : 0.25f;
+        lastDir = 0;
+        s = 0;
+      }
+      next = min(next + (unsigned)__popc(need), end);
+      need = __ballot_sync(0xffffffffu, !active);
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+    // one step of the search
+    bool done = false;
+    const float n0 = S.p.x + (S.nrm.x * S.dd) * dt;
+    const float n1 = S.p.y + (S.nrm.y * S.dd) * dt;
+    const float n2 = S.p.z + (S.nrm.z * S.dd) * dt;
+    const float n3 = S.p.w + (S.nrm.w * S.dd) * dt;
+    if (!in_bounds(d, trunc_i(n0), trunc_i(n1), trunc_i(n2), trunc_i(n3), 0)) {
+      S.dd = 9999.f;
+      done = true;
+    } else {
       const AxisW b0 = axis_index(n0, d.x), b1 = axis_index(n1, d.y);
       const AxisW b2 = axis_index(n2, d.z), b3 = axis_index(n3, d.t);
       const idx_t ni = d.index(b0.b, b1.b, b2.b, b3.b);
@@ -1100,38 +1201,47 @@ k_project_cells(float4 *__restrict__ dst, const float4 *__restrict__ vel,
         load_taps(phiOrg, ni, sY, sZ, sT, T);
         ti = ni;
       }
-      vn = ip16(T, b0, b1, b2, b3);
-      if (vn < targetVal) {
+      const float vn = ip16(T, b0, b1, b2, b3);
+      if (vn < S.target) {
         if (lastDir < 0) step *= 0.5f;
-        dd += step;
+        S.dd += step;
         lastDir = 1;
       } else {
         if (lastDir > 0) step *= 0.5f;
-        dd -= step;
+        S.dd -= step;
         lastDir = -1;
       }
       // (double)step < 0.1 equals step < 0.1f for every float: 0.1f is the
       // smallest float above 0.1.
-      if (step < 0.1f) s = lim + 1;
+      if (step < 0.1f) done = true;
     }
-    if (fabsf(dd) > threshPhi) {
-      dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
-      continue;
+    if (++s >= maxIter) done = true;
+    if (done) {
+      project_write(dst, marker, S.id, S.nrm, S.dd, threshPhi);
+      active = false;
     }
-    dst[id] = make_float4(nrm.x * dd, nrm.y * dd, nrm.z * dd, nrm.w * dd);
-    marker[id] = 1.f;
+    }
   }
 }
 
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,
-                          float threshPhi, int maxIter, cudaStream_t s) {
+                          float threshPhi, int maxIter, void *queue, unsigned int *counters,
+                          cudaStream_t s) {
   if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return;
   BoxDecoder bx = make_decoder(d.x - 4, d.y - 4, d.z - 4, 2, 2, 2, 2);
   const long long nbox = (long long)(d.x - 4) * (d.y - 4) * (d.z - 4) * (d.t - 4);
-  k_project_cells<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker,
-                                                          d, bx, (uint32_t)nbox, threshPhi,
-                                                          maxIter);
+  k_project_prep<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker, d,
+                                                         bx, (uint32_t)nbox, threshPhi, maxIter,
+                                                         (ProjState *)queue, counters);
+  k_project_search<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, phiOrg, marker, d, threshPhi,
+                                                           maxIter, (const ProjState *)queue,
+                                                           counters, counters + 1);
+}
+
+size_t project_queue_bytes(Dims4 d) {
+  if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return 16;
+  return sizeof(ProjState) * (size_t)(d.x - 4) * (d.y - 4) * (d.z - 4) * (d.t - 4);
 }
 
 // knCvExpolBlur4d (optflow4d.cpp:613-626) fused with the preceding copy:
