@@ -1029,7 +1029,7 @@ __device__ __forceinline__ void project_write(float4 *__restrict__ dst, float *_
 // and the start of the search.  Cells with a zero normal (flat, clamped phi)
 // finish here; the others are appended to `queue` (warp-aggregated, in no
 // fixed order) for k_project_search.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 5)
 k_project_prep(float4 *__restrict__ dst, const float4 *__restrict__ vel,
                const float *__restrict__ phiOrg, const float *__restrict__ phiTarget,
                float *__restrict__ marker, Dims4 d, BoxDecoder bx, uint32_t nbox,
@@ -1138,7 +1138,7 @@ k_project_prep(float4 *__restrict__ dst, const float4 *__restrict__ vel,
 // that need a cell take consecutive entries in lane order.  Every cell's
 // arithmetic is the single-cell search's, so the results do not depend on
 // which lane runs a cell.
-constexpr int PROJ_CHUNK = 256;
+constexpr int PROJ_CHUNK = 64;
 __global__ void __launch_bounds__(128)
 k_project_search(float4 *__restrict__ dst, const float *__restrict__ phiOrg,
                  float *__restrict__ marker, Dims4 d, float threshPhi, int maxIter,
@@ -1234,9 +1234,15 @@ void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
   k_project_prep<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker, d,
                                                          bx, (uint32_t)nbox, threshPhi, maxIter,
                                                          (ProjState *)queue, counters);
-  k_project_search<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, phiOrg, marker, d, threshPhi,
-                                                           maxIter, (const ProjState *)queue,
-                                                           counters, counters + 1);
+  // every block resident at once: warps leave when the queue is drained
+  static const int per_sm = [] {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_project_search, 128, 0);
+    return n < 1 ? 1 : n;
+  }();
+  k_project_search<<<sm_count() * per_sm, 128, 0, s>>>(dst, phiOrg, marker, d, threshPhi, maxIter,
+                                                       (const ProjState *)queue, counters,
+                                                       counters + 1);
 }
 
 size_t project_queue_bytes(Dims4 d) {
