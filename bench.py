@@ -516,6 +516,19 @@ def run_gpu(a):
     ctx.set_stream(stream.cuda_stream)
     W = Workload(F, synth, a.res, a.hires, a.cg_accuracy, a.blur_type, ctx)
     W.upload()
+    # The end-to-end run's pinned host buffers (3.7 GB) are allocated and
+    # filled here, seconds before they are used: on some hosts copies from
+    # freshly pinned memory ran at a tenth of the usual rate for a while.
+    pinned = {}
+    for n in ("i0", "i1", "s0", "s1", "hi0", "hi1"):
+        h = getattr(W, "h_" + n)
+        tt = torch.empty(h.shape, dtype=torch.float32, pin_memory=True)
+        tt.numpy()[...] = h
+        pinned[n] = tt.numpy()
+    pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+    sink = {"v01": pin(W.v01.shape), "v10": pin(W.v10.shape),
+            "out4": [pin(W.out4.shape) for _ in ALPHAS],
+            "frame": [pin(W.dst.shape) for _ in range(NFRAMEBUF)]}
     for _ in range(max(a.warmup, 0)):
         W.step()
     torch.cuda.synchronize()
@@ -562,17 +575,8 @@ def run_gpu(a):
     rl, share = roofline(recs, a.res, peak, peak_kind, ncu_traffic())
     rl["region"] = "profiled pass of the same steps, one CUDA event pair per launch"
 
-    # e2e: through the C ABI with pinned host buffers, copies inside
-    pinned = {}
-    for n in ("i0", "i1", "s0", "s1", "hi0", "hi1"):
-        h = getattr(W, "h_" + n)
-        tt = torch.empty(h.shape, dtype=torch.float32, pin_memory=True)
-        tt.numpy()[...] = h
-        pinned[n] = tt.numpy()
-    pin = lambda shape: torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
-    sink = {"v01": pin(W.v01.shape), "v10": pin(W.v10.shape),
-            "out4": [pin(W.out4.shape) for _ in ALPHAS],
-            "frame": [pin(W.dst.shape) for _ in range(NFRAMEBUF)]}
+    # e2e: through the C ABI with the pinned host buffers allocated above,
+    # copies inside
     def copy_rates():
         """GB/s of one hi-res input up and back down on the copy stream."""
         g = W.g_hi0
