@@ -310,8 +310,8 @@ bool launch_expol_sep_tw(const float4 *in, float4 *out, const uint16_t *mask, Di
 // ---- projection correction ------------------------------------------------------
 // knProjectCells in two kernels: the normals and the cells that finish
 // without a search, then the searches of the others, taken from `queue`
-// (project_queue_bytes(d) bytes) by whichever lane is free.  `counters` is
-// two unsigned ints, zero on entry.
+// (project_queue_bytes(d) bytes: the whole box or a t slab of it at a time)
+// by whichever lane is free.  `counters` is two unsigned ints, zero on entry.
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,
                           float threshPhi, int maxIter, void *queue, unsigned int *counters,

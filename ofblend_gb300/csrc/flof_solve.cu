@@ -1224,30 +1224,52 @@ k_project_search(float4 *__restrict__ dst, const float *__restrict__ phiOrg,
   }
 }
 
+__global__ void k_zero_counters(unsigned int *c) {
+  c[0] = 0;
+  c[1] = 0;
+}
+
+// Queue entries: the whole box, or at least PROJ_QMIN cells and a quarter of
+// the box, whichever is less; a larger box runs in t slabs of that many
+// cells.
+constexpr long long PROJ_QMIN = 16ll << 20;
+long long project_queue_cells(Dims4 d) {
+  if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return 1;
+  const long long vol = (long long)(d.x - 4) * (d.y - 4) * (d.z - 4);
+  const long long nbox = vol * (d.t - 4);
+  long long cap = nbox / 4 > PROJ_QMIN ? nbox / 4 : PROJ_QMIN;
+  if (cap < vol) cap = vol;  // at least one t plane
+  return cap < nbox ? cap : nbox;
+}
+
+size_t project_queue_bytes(Dims4 d) { return sizeof(ProjState) * (size_t)project_queue_cells(d); }
+
 void launch_project_cells(float4 *dst, const float4 *vel, const float *phiOrg,
                           const float *phiTarget, float *marker, Dims4 d,
                           float threshPhi, int maxIter, void *queue, unsigned int *counters,
                           cudaStream_t s) {
   if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return;
-  BoxDecoder bx = make_decoder(d.x - 4, d.y - 4, d.z - 4, 2, 2, 2, 2);
-  const long long nbox = (long long)(d.x - 4) * (d.y - 4) * (d.z - 4) * (d.t - 4);
-  k_project_prep<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker, d,
-                                                         bx, (uint32_t)nbox, threshPhi, maxIter,
-                                                         (ProjState *)queue, counters);
-  // every block resident at once: warps leave when the queue is drained
+  const long long vol = (long long)(d.x - 4) * (d.y - 4) * (d.z - 4);
+  const int tslab = (int)(project_queue_cells(d) / vol);  // t planes per slab
+  // every block of the search resident at once: warps leave when the queue
+  // is drained
   static const int per_sm = [] {
     int n = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_project_search, 128, 0);
     return n < 1 ? 1 : n;
   }();
-  k_project_search<<<sm_count() * per_sm, 128, 0, s>>>(dst, phiOrg, marker, d, threshPhi, maxIter,
-                                                       (const ProjState *)queue, counters,
-                                                       counters + 1);
-}
-
-size_t project_queue_bytes(Dims4 d) {
-  if (d.x < 5 || d.y < 5 || d.z < 5 || d.t < 5) return 16;
-  return sizeof(ProjState) * (size_t)(d.x - 4) * (d.y - 4) * (d.z - 4) * (d.t - 4);
+  for (int t0 = 0; t0 < d.t - 4; t0 += tslab) {
+    const int nt = min(tslab, d.t - 4 - t0);
+    const BoxDecoder bx = make_decoder(d.x - 4, d.y - 4, d.z - 4, 2, 2, 2, 2 + t0);
+    const long long nbox = vol * nt;
+    if (t0 > 0) k_zero_counters<<<1, 1, 0, s>>>(counters);
+    k_project_prep<<<grid_for(nbox, 128, 16), 128, 0, s>>>(dst, vel, phiOrg, phiTarget, marker,
+                                                           d, bx, (uint32_t)nbox, threshPhi,
+                                                           maxIter, (ProjState *)queue, counters);
+    k_project_search<<<sm_count() * per_sm, 128, 0, s>>>(dst, phiOrg, marker, d, threshPhi,
+                                                         maxIter, (const ProjState *)queue,
+                                                         counters, counters + 1);
+  }
 }
 
 // knCvExpolBlur4d (optflow4d.cpp:613-626) fused with the preceding copy:

@@ -207,6 +207,21 @@ def test_corrvelsof_bitexact(gpu, orc, dims, vscale):
     assert np.array_equal(gd.to_numpy(), want_dst)
 
 
+def test_corrvelsof_projection_slabs_bitexact(gpu, orc):
+    """A box of more than 16M cells (160^3 x 4 here) runs the projection's
+    search queue in t slabs (3 + 1 planes); one round without the blur keeps
+    the oracle's run short.  Bit for bit as one slab."""
+    dims = (164, 164, 164, 8)
+    i0, i1 = drop_pair(dims)
+    r = np.random.default_rng(29)
+    vel = (r.standard_normal(i0.shape + (4,)) * 0.5).astype(np.float32)
+    want_vel, want_dst, _ = orc.corrVelsOf4d(vel, i0, i1, 4.0, 0.0, 0.0, 40)
+    gv, gd = grid_of(vel), F.Grid4Vec4(dims=dims)
+    F.corrVelsOf4d(gd, gv, grid_of(i0), None, grid_of(i1), 4.0, -9.0, 0.0, 0.0, 40)
+    assert np.array_equal(gd.to_numpy(), want_dst)
+    assert np.array_equal(gv.to_numpy(), want_vel)
+
+
 def corner_sphere(dims, c, r):
     """lsFactor * SDF of one sphere, clamped to +-4 cells, as (T, Z, Y, X)."""
     X, Y, Z, T = dims
