@@ -122,6 +122,29 @@ def test_slab_tma_kernels_match_plain_loads(case):
         assert np.array_equal(a, b) and ea == eb, (blur, rel_l2(b, a), ea, eb)
 
 
+def test_slab_tma_kernels_match_plain_loads_odd_extents(gpu):
+    """The same on extents that leave partial tiles on every axis: x and y
+    tiles, a last z group of one plane, a last keep-mask word of three t
+    planes and a partial t walk."""
+    dims = (37, 45, 29, 23)
+    g0 = F.Grid4Real(dims=dims).from_numpy(synth.flow_input(synth.scene_for(0), dims))
+    g1 = F.Grid4Real(dims=dims).from_numpy(synth.flow_input(synth.scene_for(1), dims))
+    kw = dict(FLOF, doFinalProject=True, multiStep=1, minGridSize=100)
+    ctx = F.context()
+    for blur in (1, 2):
+        out = []
+        for tma in (1, 0):
+            ctx.set_option(_lib.FLOF_OPT_SLAB_TMA, tma)
+            try:
+                v = F.Grid4Vec4(dims=dims)
+                e = F.opticalFlowMultiscale4d(v, g0, g1, blurType=blur, **kw)
+                out.append((v.to_numpy(), e))
+            finally:
+                ctx.set_option(_lib.FLOF_OPT_SLAB_TMA, 1)
+        (a, ea), (b, eb) = out
+        assert np.array_equal(a, b) and ea == eb, (blur, rel_l2(b, a), ea, eb)
+
+
 def test_mg_params_are_checked(gpu):
     ctx = F.context()
     with pytest.raises(F.FlofError):
