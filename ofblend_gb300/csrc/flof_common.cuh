@@ -381,6 +381,22 @@ __device__ __forceinline__ float mul_inv81(float v) {
 }
 
 // ---- programmatic dependent launch (griddepcontrol, sm_90 and later) -------
+// The image gradient g at an interior cell rebuilt from the level's target
+// level set i1 with the assembly's own operations (central differences times
+// 1/(2 mDx)): the stored g bit for bit, from 4 bytes per cell instead of 16
+// (the neighbour loads hit L1 and L2).
+struct GradFromI1 {
+  const float *__restrict__ i1;
+  idx_t sY, sZ, sT;
+  float dxf;
+  __device__ __forceinline__ float4 operator()(idx_t id) const {
+    return make_float4((__ldg(i1 + id + 1) - __ldg(i1 + id - 1)) * dxf,
+                       (__ldg(i1 + id + sY) - __ldg(i1 + id - sY)) * dxf,
+                       (__ldg(i1 + id + sZ) - __ldg(i1 + id - sZ)) * dxf,
+                       (__ldg(i1 + id + sT) - __ldg(i1 + id - sT)) * dxf);
+  }
+};
+
 // pdl_wait returns once the grid this one depends on has completed and its
 // writes are visible (at once for a grid launched without the attribute);
 // pdl_launch_dependents lets the next grid of the stream be scheduled, whose

@@ -400,8 +400,8 @@ int mg_pcg(flof_ctx *c, Dims4 d, const OFConsts &k, const CGTune &tu, const OFAr
     const int n = (cap - it) < chunk ? (cap - it) : chunk;
     for (int s = 0; s < n; ++s) {
       KLP(c, KC_MATVEC, d.x, nb * 48, launch_cg_matvec(p, g, q, d, k, c->st, c->dpart, c->stream, tu));
-      KLP(c, KC_UPDATE, d.x, nb * 128,
-          launch_mgcg_update_pre(x, r, p, q, g, x0.v(), d, k, mp, c->st, c->fpart, cap,
+      KLP(c, KC_UPDATE, d.x, nb * (i1 ? 116 : 128),
+          launch_mgcg_update_pre(x, r, p, q, g, i1, x0.v(), d, k, mp, c->st, c->fpart, cap,
                                  c->stream));
       KLP(c, KC_MG, d.x, nb * 128,
           launch_mg_vcycle(r, g, x0.v(), r0.v(), z.v(), d, L.data(), nl, k, mp, c->st, c->dpart, 0,

@@ -214,11 +214,13 @@ void launch_mg_vcycle(const float4 *b0, const float4 *g, float4 *x0, float4 *r0,
 // x += alpha p, r -= alpha q, signed max of r and the stop rule.
 void launch_mgcg_update(float4 *x, float4 *r, const float4 *p, const float4 *q, Dims4 d,
                         CGState *st, float *fpart, int maxIter, cudaStream_t s);
-// The same plus the V-cycle's first level-0 sweep x0 = omega0 D^-1 r.
+// The same plus the V-cycle's first level-0 sweep x0 = omega0 D^-1 r; with
+// i1 (the level's target level set, from which the assembly built g) the
+// block solve rebuilds g from it instead of reading g.
 void launch_mgcg_update_pre(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                            const float4 *g, float4 *x0, Dims4 d, const OFConsts &c,
-                            const MGParams &mp, CGState *st, float *fpart, int maxIter,
-                            cudaStream_t s);
+                            const float4 *g, const float *i1, float4 *x0, Dims4 d,
+                            const OFConsts &c, const MGParams &mp, CGState *st, float *fpart,
+                            int maxIter, cudaStream_t s);
 // The plain operator's residual r = b - A x of a preconditioned solve (float
 // rows) and its signed maximum into the device float *rmax.
 void launch_mg_judge(const float4 *x, const float4 *b, const float4 *g, float4 *r, Dims4 d,

@@ -729,12 +729,18 @@ k_mgcg_update(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *__re
 }
 
 // k_mgcg_update plus the V-cycle's first level-0 sweep: x0 = omega D^-1 r
-// of the updated residual.
+// of the updated residual.  G gives the image gradient at a cell: the stored
+// g, or g rebuilt from i1.
+struct GradLoad {
+  const float4 *__restrict__ g;
+  __device__ __forceinline__ float4 operator()(idx_t id) const { return __ldg(g + id); }
+};
+template <class G>
 __global__ void __launch_bounds__(MT)
 k_mgcg_update_pre(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *__restrict__ p,
-                  const float4 *__restrict__ q, const float4 *__restrict__ g,
-                  float4 *__restrict__ x0, Dims4 d, BoxDecoder bx, uint32_t nint, float c0,
-                  float omega, CGState *st, float *fpart, int maxIter) {
+                  const float4 *__restrict__ q, G grad, float4 *__restrict__ x0, Dims4 d,
+                  BoxDecoder bx, uint32_t nint, float c0, float omega, CGState *st, float *fpart,
+                  int maxIter) {
   pdl_wait();
   pdl_launch_dependents();
   if (mg_stop(st)) return;
@@ -745,7 +751,7 @@ k_mgcg_update_pre(float4 *__restrict__ x, float4 *__restrict__ r, const float4 *
     int i, j, k, l;
     bx.decode(n, i, j, k, l);
     const idx_t id = d.index(i, j, k, l);
-    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = __ldg(g + id);
+    const float4 pp = __ldg(p + id), qq = __ldg(q + id), gg = grad(id);
     x[id] = f4_axpy(a, pp, x[id]);
     const float4 rr = f4_axpy(-a, qq, r[id]);
     r[id] = rr;
@@ -947,12 +953,18 @@ void launch_mgcg_update(float4 *x, float4 *r, const float4 *p, const float4 *q, 
             interior_box(d), nint, st, fpart, maxIter);
 }
 void launch_mgcg_update_pre(float4 *x, float4 *r, const float4 *p, const float4 *q,
-                            const float4 *g, float4 *x0, Dims4 d, const OFConsts &c,
-                            const MGParams &mp, CGState *st, float *fpart, int maxIter,
-                            cudaStream_t s) {
+                            const float4 *g, const float *i1, float4 *x0, Dims4 d,
+                            const OFConsts &c, const MGParams &mp, CGState *st, float *fpart,
+                            int maxIter, cudaStream_t s) {
   const uint32_t nint = interior_n(d);
-  mg_launch(k_mgcg_update_pre, grid_for(nint > 0 ? nint : 1, MT, 8), MT, s, x, r, p, q, g, x0, d,
-            interior_box(d), nint, c.diag, mp.omega0, st, fpart, maxIter);
+  const int nb = grid_for(nint > 0 ? nint : 1, MT, 8);
+  if (i1)
+    mg_launch(k_mgcg_update_pre<GradFromI1>, nb, MT, s, x, r, p, q,
+              GradFromI1{i1, d.x, d.sz(), d.st(), c.dxf}, x0, d, interior_box(d), nint, c.diag,
+              mp.omega0, st, fpart, maxIter);
+  else
+    mg_launch(k_mgcg_update_pre<GradLoad>, nb, MT, s, x, r, p, q, GradLoad{g}, x0, d,
+              interior_box(d), nint, c.diag, mp.omega0, st, fpart, maxIter);
 }
 
 void launch_mg_judge(const float4 *x, const float4 *b, const float4 *g, float4 *r, Dims4 d,

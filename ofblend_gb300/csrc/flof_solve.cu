@@ -395,17 +395,6 @@ struct GradStored {
   const T *__restrict__ g;
   __device__ __forceinline__ float4 operator()(idx_t id) const { return ld_g(g, id); }
 };
-struct GradFromI1 {
-  const float *__restrict__ i1;
-  idx_t sY, sZ, sT;
-  float dxf;
-  __device__ __forceinline__ float4 operator()(idx_t id) const {
-    return make_float4((__ldg(i1 + id + 1) - __ldg(i1 + id - 1)) * dxf,
-                       (__ldg(i1 + id + sY) - __ldg(i1 + id - sY)) * dxf,
-                       (__ldg(i1 + id + sZ) - __ldg(i1 + id - sZ)) * dxf,
-                       (__ldg(i1 + id + sT) - __ldg(i1 + id - sT)) * dxf);
-  }
-};
 
 // r -= alpha q; z = M^-1 r; sigma' = z.r; max(r).  x += alpha p is left to
 // the direction kernel (st->xpend).
