@@ -303,23 +303,6 @@ k_mg0_prolong(float4 *__restrict__ x, const float4 *__restrict__ e1, Dims4 d, Bo
 // t neighbours cost no load); z . b for the PCG: init sets sigma (and
 // beta = 0), otherwise beta = z.b / sigma and sigma = z.b.
 constexpr int MG_TT = 8;
-struct PostLoads {
-  float4 yp, zm, ym, xm, xp, yq, zp, gg, bb;
-};
-__device__ __forceinline__ void post_load(PostLoads &a, const float4 *__restrict__ b,
-                                          const float4 *__restrict__ g,
-                                          const float4 *__restrict__ y, idx_t id, idx_t sY,
-                                          idx_t sZ, idx_t sT) {
-  a.yp = __ldg(y + id + sT);
-  a.zm = __ldg(y + id - sZ);
-  a.ym = __ldg(y + id - sY);
-  a.xm = __ldg(y + id - 1);
-  a.xp = __ldg(y + id + 1);
-  a.yq = __ldg(y + id + sY);
-  a.zp = __ldg(y + id + sZ);
-  a.gg = __ldg(g + id);
-  a.bb = __ldg(b + id);
-}
 __global__ void __launch_bounds__(MT)
 k_mg0_post_tw(const float4 *__restrict__ b, const float4 *__restrict__ g,
               const float4 *__restrict__ y, float4 *__restrict__ z, Dims4 d, BoxDecoder bxyz,
