@@ -57,13 +57,14 @@ struct TG {
 template <int S> using BlurGeom = TG<S, 4, 8, 1, 1, 2>;
 using ExpolGeom = TG<1, 8, 2, 4, 2, 4, 3>;
 
-// The extrapolation sweep adds with sm_100-family packed `add.rn.f32x2`: a
-// float4 is two float pairs (x,y), (z,w), each lane rounded like the scalar
-// add, so the sums are bit for bit the scalar ones in the same order at half
-// the instruction count (4M random pairs on GB300: no difference).  The blur
-// keeps scalar multiplies and adds: a packed multiply followed by a packed add
-// gave results different from the scalar multiply-then-add in about 15% of
-// 4M random cases on GB300, which would break the reference's two roundings.
+// The extrapolation sweeps and the blur add with sm_100-family packed
+// `add.rn.f32x2`: a float4 is two float pairs (x,y), (z,w), each lane rounded
+// like the scalar add, so the sums are bit for bit the scalar ones in the
+// same order at half the instruction count (4M random pairs on GB300: no
+// difference).  The blur's products stay scalar multiplies: the packed
+// `mul.rn.f32x2` gave results different from the scalar multiply in about
+// 15% of 4M random cases on GB300, and a blur built on it failed the bitwise
+// comparisons with the reference's separately rounded products.
 struct __align__(16) P4 {
   unsigned long long lo, hi;
 };
@@ -80,14 +81,15 @@ __device__ __forceinline__ float4 unpack4(const P4 &v) {
   asm("mov.b64 {%0, %1}, %2;" : "=f"(r.z), "=f"(r.w) : "l"(v.hi));
   return r;
 }
-__device__ __forceinline__ float4 mul4(float w, const float4 &a) {
-  return make_float4(w * a.x, w * a.y, w * a.z, w * a.w);
-}
-__device__ __forceinline__ void add4(float4 &v, const float4 &p) {
-  v.x += p.x;
-  v.y += p.y;
-  v.z += p.z;
-  v.w += p.w;
+// w times a float4 by scalar multiplies, the products packed as two float
+// pairs for the packed adds
+__device__ __forceinline__ P4 mulp4(float w, const float4 &a) {
+  const float4 m = make_float4(__fmul_rn(w, a.x), __fmul_rn(w, a.y), __fmul_rn(w, a.z),
+                               __fmul_rn(w, a.w));
+  P4 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.lo) : "f"(m.x), "f"(m.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.hi) : "f"(m.z), "f"(m.w));
+  return r;
 }
 
 template <int S>
@@ -150,13 +152,13 @@ k_blur_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
 
   typedef float4 V4;
-  V4 val[DZ][DT][RY];
+  P4 val[DZ][DT][RY];  // running sums as two float pairs for the packed adds
 #pragma unroll
   for (int oz = 0; oz < DZ; ++oz)
 #pragma unroll
     for (int o = 0; o < DT; ++o)
 #pragma unroll
-      for (int q = 0; q < RY; ++q) memset(&val[oz][o][q], 0, sizeof(V4));
+      for (int q = 0; q < RY; ++q) memset(&val[oz][o][q], 0, sizeof(P4));
 
   for (int p = 0; p < NP; ++p) {
     const int vt0 = p / KZ - S, zk0 = p % KZ - S;  // offsets seen by plane (0, 0)
@@ -198,16 +200,15 @@ k_blur_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
             for (int q = 0; q < RY; ++q) used |= (k - q - S == ay) || (k - q - S == -ay);
             if (!used) continue;
             const int base = vt * vt + zk * zk + ay * ay;
-            float4 prod[2 * S + 1];
+            P4 prod[2 * S + 1];
 #pragma unroll
-            for (int xi = -S; xi <= S; ++xi)
-              prod[xi + S] = mul4(wsh[base + xi * xi], a[xi + S]);
+            for (int xi = -S; xi <= S; ++xi) prod[xi + S] = mulp4(wsh[base + xi * xi], a[xi + S]);
 #pragma unroll
             for (int q = 0; q < RY; ++q) {
               const int yj = k - q - S;
               if (yj != ay && yj != -ay) continue;
 #pragma unroll
-              for (int xi = -S; xi <= S; ++xi) add4(val[oz][o][q], prod[xi + S]);
+              for (int xi = -S; xi <= S; ++xi) acc4(val[oz][o][q], prod[xi + S]);
             }
           }
         }
@@ -233,7 +234,7 @@ k_blur_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
         const int y = y0 + RY * ty + q;
         if (y >= d.y) continue;
         const idx_t id = d.index(x, y, z, t);
-        const float4 v = val[oz][o][q];
+        const float4 v = unpack4(val[oz][o][q]);
         if (!(zt_inner && x >= 1 && x < d.x - 1 && y >= 1 && y < d.y - 1)) {
           if (zero_border) dst[id] = make_float4(0.f, 0.f, 0.f, 0.f);
           continue;
