@@ -1,17 +1,17 @@
 // flof_tma.cu -- TMA-staged slab kernels for the dense 4D stencils on Vec4
 // grids: the Gaussian velocity blur (knGaussianBlur, optflow4d.cpp:132-158,
-// radius 1 and 2) and the extrapolation sweep (knCvExpolBlur4d, :613-626).
+// radius 1 and 2) and the extrapolation sweep (knCvExpolBlur4d, :613-626),
+// direct and separable.
 //
-// Same arithmetic as flof_stencil.cu: every output sums its (2S+1)^4
-// neighbourhood in the reference's order (t, z, y, x) with float adds in
-// sequence.  A block owns a 32-column (x,y) tile at one z for DT consecutive t
-// planes and walks the input slabs those planes need once, in (t, z) order;
-// each (x,y) slab with its S-cell halo is brought into shared memory by one
-// cp.async.bulk.tensor copy issued by a single thread, completion signalled
-// on an mbarrier, with NSTAGE slabs in flight.  For the extrapolation sweep
-// four output planes share every slab, which halves the L2-to-SM traffic
-// that bounds it.  The
-// tensor map views the float4 grid as a 4D float tensor (4X, Y, Z, T), so a
+// Same arithmetic as flof_stencil.cu: every output of the blur and the direct
+// sweep sums its (2S+1)^4 neighbourhood in the reference's order (t, z, y, x)
+// with float adds in sequence.  A block owns a 32-column (x,y) tile and walks
+// the input slabs its output planes need once, in (t, z) order: the blur one
+// (z, t) plane per block, the sweeps two z planes walking t with the running
+// sums of three t planes in registers.  Each (x,y) slab with its S-cell halo
+// is brought into shared memory by one cp.async.bulk.tensor copy issued by a
+// single thread, completion signalled on an mbarrier, a few slabs in flight.
+// The tensor map views the float4 grid as a 4D float tensor (4X, Y, Z, T), so a
 // slab row is one contiguous 16W-byte run, the innermost coordinate 4x is a
 // multiple of 16 bytes for every x, and cells outside the grid arrive as
 // zeros, which leave a running float sum unchanged (a 16-byte innermost box
@@ -51,9 +51,8 @@ struct TG {
   static_assert(DZ * DT * RY <= 16, "the keep mask holds 16 cells per thread");
 };
 // The blur (S = 1, 2) is bound by its multiply-adds: one (z, t) plane per
-// block, 32 rows.  The extrapolation sweep has one add per tap and is bound by
-// how fast slabs reach shared memory and registers: four t planes and two z
-// planes share every slab (24 slabs per 8 output planes), four in flight.
+// block, 32 rows.  ExpolGeom fixes the sweeps' keep-mask layout: a 16-bit
+// word per thread for RY = 2 rows, DZ = 2 z planes and DT = 4 t planes.
 template <int S> using BlurGeom = TG<S, 4, 8, 1, 1, 2>;
 using ExpolGeom = TG<1, 8, 2, 4, 2, 4, 3>;
 
