@@ -55,8 +55,8 @@ typedef enum { FLOF_REAL = 1, FLOF_VEC4 = 8 } flof_elem;
  * 2 = separable stencils: the blur as a 4x1D stencil with the same in-bounds
  *     normalisation, and the projection's extrapolation sweep
  *     (knCvExpolBlur4d, :613-626) with its 3^4 box sum formed as 3x3 (x,y)
- *     sums added over z and t; equal to 1 up to float rounding and several
- *     times cheaper. */
+ *     sums added over z and t; equal to 1 up to float rounding, the blur
+ *     about five times and the sweep about a quarter cheaper. */
 enum { FLOF_BLUR_GAUSS = 1, FLOF_BLUR_GAUSS_SEPARABLE = 2 };
 
 typedef struct flof_ctx flof_ctx;
