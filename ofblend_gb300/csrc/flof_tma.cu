@@ -266,7 +266,9 @@ constexpr int ETW_KZ = ETW_DZ + 2;  // slabs per t plane
 static_assert(ETW_RY == ExpolGeom::RY && ETW_DZ == ExpolGeom::DZ,
               "the keep mask groups rows and z planes as the sweep does");
 
-__global__ void __launch_bounds__(32 * ETW_NW, 3)
+// Four blocks per SM (64 registers, a few bytes spilled) beat three
+// (80 registers): 0.221 against 0.229 ms per 64^4 sweep.
+__global__ void __launch_bounds__(32 * ETW_NW, 4)
 k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
            int tiles_x, const uint16_t *__restrict__ fixed, int *err) {
   extern __shared__ __align__(128) unsigned char raw[];
