@@ -1743,6 +1743,21 @@ void blend_vt(flof_ctx *c, LatsData &L, const SliceSetup &S, int zeroVel) {
   L.lastT = S.t;
 }
 
+// Both directions' blends of a two-way frame (equal deformation sizes) in
+// one launch.
+void blend_vt2(flof_ctx *c, LatsData &L0, const SliceSetup &S0, LatsData &L1,
+               const SliceSetup &S1) {
+  const flof_grid *d0 = L0.defo, *d1 = L1.defo;
+  const long long slice = (long long)d0->dims[0] * d0->dims[1] * d0->dims[2];
+  KLP(c, KC_BLEND, d0->dims[0], 2 * slice * 48,
+      launch_blend_slices2(d0->v() + (long long)S0.t * slice, d0->v() + (long long)S0.tp1 * slice,
+                           (float4 *)L0.vt, 1.0f - S0.tw, S0.tw,
+                           d1->v() + (long long)S1.t * slice, d1->v() + (long long)S1.tp1 * slice,
+                           (float4 *)L1.vt, 1.0f - S1.tw, S1.tw, slice, c->stream));
+  L0.lastT = S0.t;
+  L1.lastT = S1.t;
+}
+
 LatsData &lats_of(flof_ctx *c, int id) {
   auto it = c->lats.find(id);
   if (it == c->lats.end() || !it->second.defo)
@@ -1895,8 +1910,12 @@ FLOF_API int flof_loadAdvectTimeSlice_OptRunTwoway(
         slice_setup(L0.defo, phi0, time, loadTimeScale, defoOffset, defoScale, overrideSize);
     const SliceSetup S1 =
         slice_setup(L1.defo, phi1, time, loadTimeScale, defoOffset, defoScale, overrideSize);
-    blend_vt(c, L0, S0, 0);
-    blend_vt(c, L1, S1, 0);
+    if (&L0 != &L1) {
+      blend_vt2(c, L0, S0, L1, S1);
+    } else {  // one data set for both directions: the second blend wins, as in sequence
+      blend_vt(c, L0, S0, 0);
+      blend_vt(c, L1, S1, 0);
+    }
     const float one[4] = {1, 1, 1, 1};
     const float *dfac = defoFactor ? defoFactor : one;
     const float4 df = make_float4(dfac[0] * defoAniFac, dfac[1] * defoAniFac,

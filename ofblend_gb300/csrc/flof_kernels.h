@@ -72,6 +72,10 @@ void launch_deform_twoway(const float4 *vel, const float4 *velInv,
 // vt = (0 + f1*v1) + f2*v2 over one defo t-slice of `cells` cells
 void launch_blend_slices(const float4 *v1, const float4 *v2, float4 *vt,
                          long long cells, float f1, float f2, cudaStream_t s);
+// the same for two sets (both directions of a two-way frame) in one launch
+void launch_blend_slices2(const float4 *v1a, const float4 *v2a, float4 *vta, float fa1, float fa2,
+                          const float4 *v1b, const float4 *v2b, float4 *vtb, float fb1, float fb2,
+                          long long cells, cudaStream_t s);
 // minBnd: the KERNEL bnd of the lookup, 10 for knSemiLagrangeLookupSlice4d_
 // WithVel (OptRun), 1 for knSemiLagrangeLookupSlice4d (loadAdvectTimeSlice).
 void launch_lookup_slice(float *dst, int dx, int dy, int dz, const float *phi,

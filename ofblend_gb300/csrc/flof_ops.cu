@@ -464,6 +464,34 @@ void launch_blend_slices(const float4 *v1, const float4 *v2, float4 *vt,
   k_blend_slices<<<grid_for(cells, NT), NT, 0, s>>>(v1, v2, vt, cells, f1, f2);
 }
 
+// The blends of both directions of a two-way frame in one launch: cells of
+// the first set, then of the second, each blended as k_blend_slices does.
+struct BlendSet {
+  const float4 *v1, *v2;
+  float4 *vt;
+  float f1, f2;
+};
+__global__ void k_blend_slices2(BlendSet a, BlendSet b, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < 2 * n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const BlendSet &S = q < n ? a : b;
+    const long long e = q < n ? q : q - n;
+    const float4 x = __ldg(S.v1 + e), y = __ldg(S.v2 + e);
+    float4 r;
+    r.x = 0.f + S.f1 * x.x; r.x += S.f2 * y.x;
+    r.y = 0.f + S.f1 * x.y; r.y += S.f2 * y.y;
+    r.z = 0.f + S.f1 * x.z; r.z += S.f2 * y.z;
+    r.w = 0.f + S.f1 * x.w; r.w += S.f2 * y.w;
+    S.vt[e] = r;
+  }
+}
+void launch_blend_slices2(const float4 *v1a, const float4 *v2a, float4 *vta, float fa1, float fa2,
+                          const float4 *v1b, const float4 *v2b, float4 *vtb, float fb1, float fb2,
+                          long long cells, cudaStream_t s) {
+  k_blend_slices2<<<grid_for(2 * cells, NT), NT, 0, s>>>(BlendSet{v1a, v2a, vta, fa1, fa2},
+                                                         BlendSet{v1b, v2b, vtb, fb1, fb2}, cells);
+}
+
 __device__ __forceinline__ float lookup_one(const float *__restrict__ phi, const Dims4 &pd,
                                             float time, float dt,
                                             const float4 *__restrict__ vt, int vx,
