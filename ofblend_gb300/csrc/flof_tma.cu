@@ -414,9 +414,14 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
 // shared-memory or DRAM bandwidth, so warps count most: at 64^4 on GB300,
 // RY = 2 rows per thread (8 warps, three blocks per SM) took 0.168 ms a
 // sweep against 0.178 ms for RY = 4 (4 warps), and TC = 4 or deeper slab
-// pipelines did not help.
-constexpr int ESW_RY = 2, ESW_NW = ETW_TY / ESW_RY, ESW_TC = 8, ESW_NS = 4, ESW_MINB = 3;
-constexpr int ESW_SMEM = ESW_NS * ETW_STRIDE;
+// pipelines did not help.  A copy brings two z slabs (one block barrier per
+// two slabs): 0.165 ms.
+constexpr int ESW_RY = 2, ESW_NW = ETW_TY / ESW_RY, ESW_TC = 8, ESW_NS = 3, ESW_MINB = 3;
+constexpr int ESW_SPC = 2;  // z slabs per copy: one barrier step per two slabs
+constexpr int ESW_CBYTES = ESW_SPC * ETW_BYTES;  // one copy, its slabs back to back
+constexpr int ESW_CSTRIDE = (ESW_CBYTES + 127) / 128 * 128;
+constexpr int ESW_SMEM = ESW_NS * ESW_CSTRIDE;
+static_assert(ETW_KZ % ESW_SPC == 0, "whole copies per plane");
 
 __global__ void __launch_bounds__(32 * ESW_NW, ESW_MINB)
 k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
@@ -439,12 +444,13 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  const int NP = (ESW_TC + 2) * KZ;  // slab p: plane t0 - 1 + p / KZ, z0 - 1 + p % KZ
+  constexpr int CPP = KZ / ESW_SPC;   // copies per t plane
+  const int NP = (ESW_TC + 2) * CPP;  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
   auto issue = [&](int p) {
     uint64_t *b = &bar[p % NS];
-    mbar_expect_tx(b, ETW_BYTES);
-    tma_load_slab(raw + (p % NS) * ETW_STRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + p % KZ,
-                  t0 - 1 + p / KZ, b);
+    mbar_expect_tx(b, ESW_CBYTES);
+    tma_load_slab(raw + (p % NS) * ESW_CSTRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + ESW_SPC * (p % CPP),
+                  t0 - 1 + p / CPP, b);
   };
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -466,13 +472,17 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
                                      d.x + x));
     }
 #pragma unroll
-    for (int zk = 0; zk < KZ; ++zk) {
-      const int p = j * KZ + zk;
+    for (int zc = 0; zc < CPP; ++zc) {
+      const int p = j * CPP + zc;
       if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
       // A thread whose wait gave up still reads the buffer (stale values,
-      // in bounds); the barrier that ends the slab's step then ends the block.
+      // in bounds); the barrier that ends the copy's step then ends the block.
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
-      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE) + RY * ty * ETW_W + tx;
+#pragma unroll
+      for (int sl = 0; sl < ESW_SPC; ++sl) {
+      const int zk = zc * ESW_SPC + sl;
+      const P4 *cur = (const P4 *)(raw + (p % NS) * ESW_CSTRIDE + sl * ETW_BYTES) + RY * ty * ETW_W +
+                      tx;
       auto xsum = [&](int k) {
         const P4 *row = cur + k * ETW_W;
         P4 v = row[0];
@@ -495,6 +505,7 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
         }
         r0 = r1;
         r1 = r2;
+      }
       }
       if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) {
@@ -556,14 +567,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 // Tensor map of a float4 grid as a 4D float tensor (4X, Y, Z, T) with a
 // (4W, H, 1, 1) box: each slab row is one contiguous run of 16W bytes.
-bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H) {
+bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H, int D) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn || ((uintptr_t)base & 15) || 4 * W > 256) return false;
   const cuuint64_t dims[4] = {(cuuint64_t)4 * d.x, (cuuint64_t)d.y, (cuuint64_t)d.z,
                               (cuuint64_t)d.t};
   const cuuint64_t strides[3] = {(cuuint64_t)16 * d.x, (cuuint64_t)16 * d.x * d.y,
                                  (cuuint64_t)16 * d.x * d.y * d.z};
-  const cuuint32_t box[4] = {(cuuint32_t)(4 * W), (cuuint32_t)H, 1, 1};
+  const cuuint32_t box[4] = {(cuuint32_t)(4 * W), (cuuint32_t)H, (cuuint32_t)D, 1};
   const cuuint32_t es[4] = {1, 1, 1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void *)base, dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -681,7 +692,7 @@ bool launch_expol_sep_tw(const float4 *in, float4 *out, const uint16_t *mask, Di
   const int zgroups = (d.z + ETW_DZ - 1) / ETW_DZ, tgroups = (d.t + ESW_TC - 1) / ESW_TC;
   if (zgroups > 65535 || tgroups > 65535) return false;
   CUtensorMap map;
-  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H)) return false;
+  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H, ESW_SPC)) return false;
   static const bool attr = [] {
     if (cudaFuncSetAttribute(k_expol_sep_tw, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              ESW_SMEM) != cudaSuccess) {

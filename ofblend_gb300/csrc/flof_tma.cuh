@@ -53,8 +53,9 @@ __device__ __forceinline__ void tma_load_slab(void *dst, const CUtensorMap *map,
 }
 
 // Tensor map of the float4 grid at base as a 4D float tensor (4X, Y, Z, T)
-// with a (4W, H, 1, 1) box; false when the driver entry point is missing,
-// base is not 16-byte aligned or 4W exceeds 256.
-bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H);
+// with a (4W, H, D, 1) box (D consecutive z slabs per copy); false when the
+// driver entry point is missing, base is not 16-byte aligned or 4W exceeds
+// 256.
+bool encode_slab_map(CUtensorMap *m, const float4 *base, Dims4 d, int W, int H, int D = 1);
 
 }  // namespace flof
