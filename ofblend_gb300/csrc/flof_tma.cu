@@ -256,18 +256,21 @@ k_blur_tma(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
 // tt + 1 (which starts there).  Every output thus adds its 81 taps in the
 // reference's order (t, z, y, x) with float adds in sequence, and the loop
 // body is the same for every plane: no run-time choice of outputs.
-constexpr int ETW_NW = 8, ETW_RY = 2, ETW_DZ = 2, ETW_TC = 8, ETW_NS = 4;
+constexpr int ETW_NW = 8, ETW_RY = 2, ETW_DZ = 2, ETW_TC = 8, ETW_NS = 2;
 constexpr int ETW_TY = ETW_NW * ETW_RY;
 constexpr int ETW_W = TX + 2, ETW_H = ETW_TY + 2;
 constexpr int ETW_BYTES = ETW_W * ETW_H * 16;
-constexpr int ETW_STRIDE = (ETW_BYTES + 127) / 128 * 128;
-constexpr int ETW_SMEM = ETW_NS * ETW_STRIDE;
+constexpr int ETW_SPC = 2;  // z slabs per copy of the direct sweep
+constexpr int ETW_CBYTES = ETW_SPC * ETW_BYTES;
+constexpr int ETW_CSTRIDE = (ETW_CBYTES + 127) / 128 * 128;
+constexpr int ETW_SMEM = ETW_NS * ETW_CSTRIDE;
 constexpr int ETW_KZ = ETW_DZ + 2;  // slabs per t plane
 static_assert(ETW_RY == ExpolGeom::RY && ETW_DZ == ExpolGeom::DZ,
               "the keep mask groups rows and z planes as the sweep does");
 
 // Four blocks per SM (64 registers, a few bytes spilled) beat three
-// (80 registers): 0.221 against 0.229 ms per 64^4 sweep.
+// (80 registers): 0.221 against 0.229 ms per 64^4 sweep; copies of two z
+// slabs, two copies in flight (one barrier per two slabs), 0.217 ms.
 __global__ void __launch_bounds__(32 * ETW_NW, 4)
 k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Dims4 d,
            int tiles_x, const uint16_t *__restrict__ fixed, int *err) {
@@ -289,12 +292,13 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
-  const int NP = (ETW_TC + 2) * KZ;  // slab p: plane t0 - 1 + p / KZ, z0 - 1 + p % KZ
+  constexpr int CPP = KZ / ETW_SPC;   // copies per t plane
+  const int NP = (ETW_TC + 2) * CPP;  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
   auto issue = [&](int p) {
     uint64_t *b = &bar[p % NS];
-    mbar_expect_tx(b, ETW_BYTES);
-    tma_load_slab(raw + (p % NS) * ETW_STRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + p % KZ,
-                  t0 - 1 + p / KZ, b);
+    mbar_expect_tx(b, ETW_CBYTES);
+    tma_load_slab(raw + (p % NS) * ETW_CSTRIDE, &map, x0 - 1, y0 - 1, z0 - 1 + ETW_SPC * (p % CPP),
+                  t0 - 1 + p / CPP, b);
   };
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -314,14 +318,17 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
         for (int q = 0; q < RY; ++q) memset(&C[oz][q], 0, sizeof(P4));
     }
 #pragma unroll
-    for (int zk = 0; zk < KZ; ++zk) {
-      const int p = j * KZ + zk;
-      // buffer (p - 1) % NS was released by the barrier that ended slab p - 1
+    for (int zc = 0; zc < CPP; ++zc) {
+      const int p = j * CPP + zc;
+      // buffer (p - 1) % NS was released by the barrier that ended copy p - 1
       if (threadIdx.x == 0 && p + NS - 1 < NP) issue(p + NS - 1);
       // A thread whose wait gave up still reads the buffer (stale values, in
-      // bounds); the barrier that ends the slab's step then ends the block.
+      // bounds); the barrier that ends the copy's step then ends the block.
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
-      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_STRIDE);
+#pragma unroll
+      for (int sl = 0; sl < ETW_SPC; ++sl) {
+      const int zk = zc * ETW_SPC + sl;
+      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_CSTRIDE + sl * ETW_BYTES);
 #pragma unroll
       for (int k = 0; k < RY + 2; ++k) {
         const P4 *row = cur + (RY * ty + k) * ETW_W + tx;
@@ -352,6 +359,7 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
             }
           }
         }
+      }
       }
       if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) {
@@ -671,7 +679,7 @@ bool launch_expol_tw(const float4 *in, float4 *out, const uint16_t *mask, Dims4 
   const int zgroups = (d.z + ETW_DZ - 1) / ETW_DZ, tgroups = (d.t + ETW_TC - 1) / ETW_TC;
   if (zgroups > 65535 || tgroups > 65535) return false;
   CUtensorMap map;
-  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H)) return false;
+  if (!encode_slab_map(&map, in, d, ETW_W, ETW_H, ETW_SPC)) return false;
   static const bool attr = [] {
     if (cudaFuncSetAttribute(k_expol_tw, cudaFuncAttributeMaxDynamicSharedMemorySize, ETW_SMEM) !=
         cudaSuccess) {
