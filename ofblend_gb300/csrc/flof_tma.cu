@@ -327,39 +327,39 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
 #pragma unroll
       for (int sl = 0; sl < ETW_SPC; ++sl) {
-      const int zk = zc * ETW_SPC + sl;
-      const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_CSTRIDE + sl * ETW_BYTES);
+        const int zk = zc * ETW_SPC + sl;
+        const P4 *cur = (const P4 *)(raw + (p % NS) * ETW_CSTRIDE + sl * ETW_BYTES);
 #pragma unroll
-      for (int k = 0; k < RY + 2; ++k) {
-        const P4 *row = cur + (RY * ty + k) * ETW_W + tx;
-        const P4 a0 = row[0], a1 = row[1], a2 = row[2];
+        for (int k = 0; k < RY + 2; ++k) {
+          const P4 *row = cur + (RY * ty + k) * ETW_W + tx;
+          const P4 a0 = row[0], a1 = row[1], a2 = row[2];
 #pragma unroll
-        for (int oz = 0; oz < DZ; ++oz) {
-          const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
-          if (zrel < -1 || zrel > 1) continue;
+          for (int oz = 0; oz < DZ; ++oz) {
+            const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
+            if (zrel < -1 || zrel > 1) continue;
 #pragma unroll
-          for (int q = 0; q < RY; ++q) {
-            const int yj = k - q - 1;
-            if (yj < -1 || yj > 1) continue;
-            // vt = -1 of output tt + 1, vt = 0 of output tt, vt = +1 of output tt - 1
-            if (DC) {
-              acc4(C[oz][q], a0);
-              acc4(C[oz][q], a1);
-              acc4(C[oz][q], a2);
-            }
-            if (DB) {
-              acc4(B[oz][q], a0);
-              acc4(B[oz][q], a1);
-              acc4(B[oz][q], a2);
-            }
-            if (DA) {
-              acc4(A[oz][q], a0);
-              acc4(A[oz][q], a1);
-              acc4(A[oz][q], a2);
+            for (int q = 0; q < RY; ++q) {
+              const int yj = k - q - 1;
+              if (yj < -1 || yj > 1) continue;
+              // vt = -1 of output tt + 1, vt = 0 of output tt, vt = +1 of output tt - 1
+              if (DC) {
+                acc4(C[oz][q], a0);
+                acc4(C[oz][q], a1);
+                acc4(C[oz][q], a2);
+              }
+              if (DB) {
+                acc4(B[oz][q], a0);
+                acc4(B[oz][q], a1);
+                acc4(B[oz][q], a2);
+              }
+              if (DA) {
+                acc4(A[oz][q], a0);
+                acc4(A[oz][q], a1);
+                acc4(A[oz][q], a2);
+              }
             }
           }
         }
-      }
       }
       if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) {
@@ -488,32 +488,32 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
       const bool ok = mbar_wait_bounded(&bar[p % NS], (p / NS) & 1);
 #pragma unroll
       for (int sl = 0; sl < ESW_SPC; ++sl) {
-      const int zk = zc * ESW_SPC + sl;
-      const P4 *cur = (const P4 *)(raw + (p % NS) * ESW_CSTRIDE + sl * ETW_BYTES) + RY * ty * ETW_W +
-                      tx;
-      auto xsum = [&](int k) {
-        const P4 *row = cur + k * ETW_W;
-        P4 v = row[0];
-        acc4(v, row[1]);
-        acc4(v, row[2]);
-        return v;
-      };
-      P4 r0 = xsum(0), r1 = xsum(1);
+        const int zk = zc * ESW_SPC + sl;
+        const P4 *cur =
+            (const P4 *)(raw + (p % NS) * ESW_CSTRIDE + sl * ETW_BYTES) + RY * ty * ETW_W + tx;
+        auto xsum = [&](int k) {
+          const P4 *row = cur + k * ETW_W;
+          P4 v = row[0];
+          acc4(v, row[1]);
+          acc4(v, row[2]);
+          return v;
+        };
+        P4 r0 = xsum(0), r1 = xsum(1);
 #pragma unroll
-      for (int q = 0; q < RY; ++q) {
-        const P4 r2 = xsum(q + 2);
-        P4 xy = r0;
-        acc4(xy, r1);
-        acc4(xy, r2);
+        for (int q = 0; q < RY; ++q) {
+          const P4 r2 = xsum(q + 2);
+          P4 xy = r0;
+          acc4(xy, r1);
+          acc4(xy, r2);
 #pragma unroll
-        for (int oz = 0; oz < DZ; ++oz) {
-          const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
-          if (zrel == -1) Zc[oz][q] = xy;
-          else if (zrel <= 1) acc4(Zc[oz][q], xy);
+          for (int oz = 0; oz < DZ; ++oz) {
+            const int zrel = zk - 1 - oz;  // this slab's z offset from output plane z0 + oz
+            if (zrel == -1) Zc[oz][q] = xy;
+            else if (zrel <= 1) acc4(Zc[oz][q], xy);
+          }
+          r0 = r1;
+          r1 = r2;
         }
-        r0 = r1;
-        r1 = r2;
-      }
       }
       if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) {
