@@ -293,7 +293,8 @@ k_expol_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst, Di
   }
   __syncthreads();
   constexpr int CPP = KZ / ETW_SPC;   // copies per t plane
-  const int NP = (ETW_TC + 2) * CPP;  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
+  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
+  const int NP = (ETW_TC + 2) * CPP;
   auto issue = [&](int p) {
     uint64_t *b = &bar[p % NS];
     mbar_expect_tx(b, ETW_CBYTES);
@@ -453,7 +454,8 @@ k_expol_sep_tw(const __grid_constant__ CUtensorMap map, float4 *__restrict__ dst
   }
   __syncthreads();
   constexpr int CPP = KZ / ESW_SPC;   // copies per t plane
-  const int NP = (ESW_TC + 2) * CPP;  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
+  // copy p: plane t0 - 1 + p / CPP, slabs from z0 - 1 + SPC (p % CPP)
+  const int NP = (ESW_TC + 2) * CPP;
   auto issue = [&](int p) {
     uint64_t *b = &bar[p % NS];
     mbar_expect_tx(b, ESW_CBYTES);
