@@ -347,9 +347,9 @@ FLOF_API int flof_deform4d(flof_ctx *ctx, flof_grid *out, const flof_grid *i0,
  * Its scratch is a fixed 8 KiB device array in the library (1024 block
  * partials plus a counter), held by every GPU that loads the library until
  * exit and shared by all calls: calls that overlap on the GPU race on it.
- * Outside stream capture every call looks the array's address up for the
- * current context; a captured call uses the address of the last ordinary
- * call on that device, so make an ordinary call first. */
+ * Every call looks the array's address up for the current context, except
+ * while its stream is being captured, when the address found by the last
+ * call on that device is used. */
 FLOF_API int flof_calcLsDiff4d_noalloc(const float *i0, const float *i1,
                                        float *out, const int dims[4],
                                        float correction, int bnd,
